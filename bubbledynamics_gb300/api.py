@@ -1,0 +1,298 @@
+"""Python host layer over libbubbledyn (include/bubbledyn.h).
+
+Each method maps one-to-one onto a C entry point.  There is no CPU fallback:
+if the compiled library is missing, `load()` raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi
+from .presets import WesterveltProblem
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "lib", "libbubbledyn.so")
+
+P = C.c_void_p
+_lib = None
+
+# numpy mirrors of the bulk structs (same layout as the C structs)
+BUBBLE_DTYPE = np.dtype([("R0", "f8"), ("n_tones", "i4"), ("pad0", "i4"),
+                         ("f", "f8", (abi.BD_MAX_BUBBLE_TONES,)), ("a", "f8", (abi.BD_MAX_BUBBLE_TONES,)),
+                         ("phi", "f8", (abi.BD_MAX_BUBBLE_TONES,))])
+RESULT_DTYPE = np.dtype([("R", "f8"), ("Rdot", "f8"), ("tau", "f8"), ("q", "f8"), ("t", "f8"),
+                         ("R_max", "f8"), ("R_min", "f8"), ("t_threshold", "f8"),
+                         ("n_accept", "i8"), ("n_reject", "i8"), ("status", "i4"), ("threshold", "i4")])
+assert BUBBLE_DTYPE.itemsize == C.sizeof(abi.Bubble)
+assert RESULT_DTYPE.itemsize == C.sizeof(abi.BubbleResult)
+
+
+class BDError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("%s: %s" % (abi.STATUS_NAMES.get(status, status), msg))
+        self.status = status
+
+
+def _sig(L, name, args, res=C.c_int):
+    f = getattr(L, name)
+    f.argtypes = args
+    f.restype = res
+
+
+def load(path=None):
+    """Load the compiled library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise RuntimeError("libbubbledyn.so not found at %s: run __graft_entry__.build() "
+                           "(there is no CPU fallback)" % path)
+    L = C.CDLL(path)
+    _sig(L, "bd_context_create", [C.c_int, C.POINTER(P)])
+    _sig(L, "bd_context_destroy", [P])
+    _sig(L, "bd_last_error_string", [], C.c_char_p)
+    _sig(L, "bd_abi_version", [])
+    _sig(L, "bd_context_kernel_launches", [P, C.POINTER(C.c_int64)])
+    _sig(L, "bd_westervelt_run", [P, P, P, P, P, P])
+    _sig(L, "bd_westervelt_begin", [P, P, P, P, P, C.POINTER(P)])
+    _sig(L, "bd_westervelt_advance", [P, C.c_int64])
+    _sig(L, "bd_westervelt_step_index", [P, C.POINTER(C.c_int64)])
+    _sig(L, "bd_westervelt_finish", [P, P])
+    _sig(L, "bd_westervelt_end", [P])
+    _sig(L, "bd_westervelt_last_ms", [P, C.POINTER(C.c_double)])
+    _sig(L, "bd_checkpoint_size", [P, C.POINTER(C.c_size_t)])
+    _sig(L, "bd_checkpoint_save", [P, P, C.c_size_t])
+    _sig(L, "bd_checkpoint_load", [P, P, C.c_size_t])
+    _sig(L, "bd_trajectory_shifts", [P, P, P, C.c_int64, C.POINTER(C.c_int64), P, C.c_int32])
+    _sig(L, "bd_unfold_quarter", [P, C.c_int32, C.c_int32, P])
+    _sig(L, "bd_spiral_heat_run", [P, P, P, P, C.c_int64, P])
+    _sig(L, "bd_gilmore_combo_tones", [C.c_double, P, P, P])
+    _sig(L, "bd_gilmore_combos", [C.c_int32, C.c_double, C.c_double, P, C.c_int64, C.POINTER(C.c_int64)])
+    _sig(L, "bd_gilmore_run", [P, P, C.c_int64, P, P, P, C.POINTER(C.c_double)])
+    _sig(L, "bd_gilmore_run_device", [P, P, C.c_int64, P, P, P, P])
+    _sig(L, "bd_gilmore_threshold", [P, P, P, C.c_int64, P, C.c_int64, C.c_int32, C.c_int64, P,
+                                     C.POINTER(C.c_double)])
+    if hasattr(L, "bd_westervelt_adjoint"):
+        _sig(L, "bd_westervelt_adjoint", [P, P, P, P, P, P, C.POINTER(C.c_double), P, P, P])
+    _lib = L
+    return L
+
+
+def check(st):
+    if st != abi.BD_OK:
+        raise BDError(st, load().bd_last_error_string().decode(errors="replace"))
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data
+
+
+def trajectory_shifts(traj, leg_cap=4096):
+    """Per-step (sx, sy) shifts and the step count after each leg/spot."""
+    L = load()
+    n = C.c_int64(0)
+    check(L.bd_trajectory_shifts(C.byref(traj), None, None, 0, C.byref(n), None, 0))
+    sx = np.zeros(max(n.value, 1), np.int32)
+    sy = np.zeros(max(n.value, 1), np.int32)
+    legs = np.zeros(leg_cap, np.int64)
+    check(L.bd_trajectory_shifts(C.byref(traj), _ptr(sx), _ptr(sy), n.value, C.byref(n), _ptr(legs), leg_cap))
+    nl = traj.n_spots if traj.kind == abi.BD_TRAJ_SPOTS else traj.n_legs
+    return sx[:n.value], sy[:n.value], legs[:nl]
+
+
+def unfold_quarter(small, n_half, nz):
+    L = load()
+    small = np.ascontiguousarray(small, dtype=np.float64)
+    nf = 2 * n_half + 1
+    full = np.zeros(nz * nf * nf, np.float64)
+    check(L.bd_unfold_quarter(_ptr(small), n_half, nz, _ptr(full)))
+    return full.reshape(nz, nf, nf)
+
+
+def gilmore_combos(n_fr=55, f_min=0.02e6, f_max=5.0e6):
+    L = load()
+    n = C.c_int64(0)
+    check(L.bd_gilmore_combos(n_fr, f_min, f_max, None, 0, C.byref(n)))
+    out = np.zeros(3 * n.value, np.float64)
+    check(L.bd_gilmore_combos(n_fr, f_min, f_max, _ptr(out), n.value, C.byref(n)))
+    return out.reshape(n.value, 3)
+
+
+class Context:
+    """A device context (stream, events, device memory pool)."""
+
+    def __init__(self, device=0):
+        self.L = load()
+        h = P()
+        check(self.L.bd_context_create(device, C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.L.bd_context_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def kernel_launches(self):
+        n = C.c_int64(0)
+        check(self.L.bd_context_kernel_launches(self.h, C.byref(n)))
+        return n.value
+
+    # ------------------------------------------------------------ Westervelt
+    @staticmethod
+    def _outputs(prob, want):
+        dt = prob.dtype
+        n = prob.ncell
+        out = abi.WesterveltOutputs()
+        res = {}
+        for k in ("p_final", "peak", "energy"):
+            if k in want:
+                res[k] = np.zeros(n, dt)
+                setattr(out, k, _ptr(res[k]))
+        p = prob.params
+        if "dft" in want and p.n_dft > 0:
+            nz = max(0, min(prob.grid.nz, p.dft_z_hi) - max(0, p.dft_z_lo))
+            m = p.n_dft * prob.grid.nx * prob.grid.ny * nz
+            res["dft_re"] = np.zeros(m, dt)
+            res["dft_im"] = np.zeros(m, dt)
+            out.dft_re = _ptr(res["dft_re"])
+            out.dft_im = _ptr(res["dft_im"])
+        if "Q" in want and p.q_mode == abi.BD_Q_REFERENCE:
+            res["Q"] = np.zeros(n, np.float64)
+            out.Q = _ptr(res["Q"])
+        return out, res
+
+    @staticmethod
+    def _shape(prob, res, out):
+        for k in ("p_final", "peak", "energy", "Q"):
+            if k in res:
+                res[k] = res[k].reshape(prob.shape)
+        res["elapsed_ms"] = out.elapsed_ms
+        res["steps_done"] = out.steps_done
+        return res
+
+    def westervelt(self, prob: WesterveltProblem, want=("p_final", "peak", "energy", "Q", "dft")):
+        """Full solve (bd_westervelt_run); returns the requested host arrays."""
+        out, res = self._outputs(prob, want)
+        check(self.L.bd_westervelt_run(self.h, C.byref(prob.grid), C.byref(prob.medium), C.byref(prob.source),
+                                       C.byref(prob.params), C.byref(out)))
+        return self._shape(prob, res, out)
+
+    def westervelt_session(self, prob: WesterveltProblem):
+        return WesterveltSession(self, prob)
+
+    # ------------------------------------------------------------ heat
+    def heat(self, thermal, Q, traj, max_steps=0, snapshot_legs=(), want_T=True, want_dose=True):
+        n = thermal.nx * thermal.ny * thermal.nz
+        Q = np.ascontiguousarray(Q, dtype=np.float64).reshape(-1)
+        assert Q.size == n
+        out = abi.HeatOutputs()
+        res = {}
+        if want_T:
+            res["T"] = np.zeros(n, np.float64)
+            out.T_final = _ptr(res["T"])
+        if want_dose:
+            res["dose"] = np.zeros(n, np.float64)
+            out.dose = _ptr(res["dose"])
+        legs = np.ascontiguousarray(snapshot_legs, dtype=np.int32)
+        if legs.size:
+            res["snapshots"] = np.zeros((legs.size, n), np.float64)
+            out.snapshots = _ptr(res["snapshots"])
+            out.snapshot_legs = _ptr(legs)
+            out.n_snap = legs.size
+        check(self.L.bd_spiral_heat_run(self.h, C.byref(thermal), _ptr(Q), C.byref(traj), max_steps, C.byref(out)))
+        shp = (thermal.nz, thermal.ny, thermal.nx)
+        for k in ("T", "dose"):
+            if k in res:
+                res[k] = res[k].reshape(shp)
+        if "snapshots" in res:
+            res["snapshots"] = res["snapshots"].reshape((legs.size,) + shp)
+        res["elapsed_ms"] = out.elapsed_ms
+        res["steps_done"] = out.steps_done
+        return res
+
+    # ------------------------------------------------------------ Gilmore
+    def gilmore(self, medium, bubbles, ode):
+        """bubbles: numpy array of BUBBLE_DTYPE; returns (results RESULT_DTYPE, device ms)."""
+        bubbles = np.ascontiguousarray(bubbles, dtype=BUBBLE_DTYPE)
+        res = np.zeros(bubbles.size, RESULT_DTYPE)
+        ms = C.c_double(0)
+        check(self.L.bd_gilmore_run(self.h, C.byref(medium), bubbles.size, _ptr(bubbles), C.byref(ode),
+                                    _ptr(res), C.byref(ms)))
+        return res, ms.value
+
+    def gilmore_threshold(self, medium, fr_combo, R0, ref_arith=1, max_steps=0):
+        fr = np.ascontiguousarray(fr_combo, dtype=np.float64).reshape(-1)
+        R0 = np.ascontiguousarray(R0, dtype=np.float64)
+        nc = fr.size // 3
+        out = np.zeros(nc * R0.size, np.float64)
+        ms = C.c_double(0)
+        check(self.L.bd_gilmore_threshold(self.h, C.byref(medium), _ptr(fr), nc, _ptr(R0), R0.size, ref_arith,
+                                          max_steps, _ptr(out), C.byref(ms)))
+        return out.reshape(nc, R0.size), ms.value
+
+
+class WesterveltSession:
+    """bd_westervelt_begin / advance / checkpoint / finish / end."""
+
+    def __init__(self, ctx: Context, prob: WesterveltProblem):
+        self.ctx = ctx
+        self.prob = prob
+        self.L = ctx.L
+        h = P()
+        check(self.L.bd_westervelt_begin(ctx.h, C.byref(prob.grid), C.byref(prob.medium), C.byref(prob.source),
+                                         C.byref(prob.params), C.byref(h)))
+        self.h = h
+
+    def advance(self, n):
+        check(self.L.bd_westervelt_advance(self.h, int(n)))
+
+    def step(self):
+        s = C.c_int64(0)
+        check(self.L.bd_westervelt_step_index(self.h, C.byref(s)))
+        return s.value
+
+    def last_ms(self):
+        v = C.c_double(0)
+        check(self.L.bd_westervelt_last_ms(self.h, C.byref(v)))
+        return v.value
+
+    def checkpoint(self):
+        n = C.c_size_t(0)
+        check(self.L.bd_checkpoint_size(self.h, C.byref(n)))
+        blob = np.zeros(n.value, np.uint8)
+        check(self.L.bd_checkpoint_save(self.h, _ptr(blob), n.value))
+        return blob
+
+    def restore(self, blob):
+        blob = np.ascontiguousarray(blob, dtype=np.uint8)
+        check(self.L.bd_checkpoint_load(self.h, _ptr(blob), blob.size))
+
+    def finish(self, want=("p_final", "peak", "energy", "Q", "dft")):
+        out, res = Context._outputs(self.prob, want)
+        check(self.L.bd_westervelt_finish(self.h, C.byref(out)))
+        return Context._shape(self.prob, res, out)
+
+    def close(self):
+        if self.h:
+            self.L.bd_westervelt_end(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

@@ -1,0 +1,372 @@
+// Bioheat + CEM43 dose along a scan trajectory: bd_spiral_heat_run and
+// bd_trajectory_shifts.  Replaces T:52-105 (kernel) and T:323-573 (host loop).
+//
+// BD_F64: temperature in double, dose increment pow(4|2, T-43) dt exactly as
+//         T:99-102 (reference-faithful mode).
+// BD_F32: theta = T - T_ref in float (the per-step change of about 1e-4 K would
+//         be lost against 300 K in float), source Q in float, and the dose kept
+//         as a double-float pair (hi + lo, ~48-bit mantissa) updated with
+//         error-free FP32 sums, because FP64 arithmetic is the scarce unit on
+//         this GPU.  Traffic: theta read + write 8 B, Q 4 B, dose RMW 16 B.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "bd_internal.h"
+
+namespace bd {
+
+template <class real>
+struct HeatMat {
+    real a0;        // 1 - 4 kxy - 2 kz - w dt
+    real kxy, kz;   // dt k/(rho c dx^2), dt k/(rho c dz^2)  (T:212-215)
+    real qc;        // dt/(rho c)                              (T:216-217)
+    real wTa;       // w dt (T_art - T_ref)
+};
+
+template <class real>
+struct HeatArgs {
+    int nx, ny, nz, zb;
+    long long plane;
+    const real* __restrict__ Tin;
+    real* __restrict__ Tout;
+    const real* __restrict__ Q;
+    double* __restrict__ TD;       // BD_F64 dose
+    float2* __restrict__ TDf;      // BD_F32 dose (hi, lo)
+    const int* __restrict__ plane_mat;
+    const uint8_t* __restrict__ matmap;
+    const int2* __restrict__ shifts;   // per step (sx, sy)
+    const long long* __restrict__ step_base;
+    HeatMat<real> mat[BD_MAX_MATERIALS];
+    real dt;
+    double T_ref;
+    float T_refm43;                // T_ref - 273.15 - 43
+};
+
+// error-free a + b (Knuth TwoSum) on floats
+__device__ __forceinline__ float2 two_sum(float a, float b) {
+    const float s = a + b;
+    const float bb = s - a;
+    const float e = (a - (s - bb)) + (b - bb);
+    return make_float2(s, e);
+}
+
+// double-float accumulate: (hi, lo) += x
+__device__ __forceinline__ float2 df_add(float2 d, float x) {
+    float2 s = two_sum(d.x, x);
+    const float lo = s.y + d.y;
+    const float hi = s.x + lo;
+    return make_float2(hi, lo - (hi - s.x));
+}
+
+template <class real>
+__global__ void heat_step_kernel(const HeatArgs<real> a, int koff) {
+    const int ix = blockIdx.x * blockDim.x + threadIdx.x;
+    const int iy = blockIdx.y * blockDim.y + threadIdx.y;
+    // interior only (T:65); faces keep their initial value
+    if (ix < 1 || iy < 1 || ix >= a.nx - 1 || iy >= a.ny - 1) return;
+    const long long step = *a.step_base + koff;
+    const int2 sh = a.shifts[step];
+    const int ixa = ix - sh.x, iya = iy - sh.y;                  // T:61-62
+    const bool qin = ixa >= 0 && ixa < a.nx && iya >= 0 && iya < a.ny;
+    const long long col = (long long)iy * a.nx + ix;
+    const long long colq = (long long)iya * a.nx + ixa;
+    const int z0 = max(1, blockIdx.z * a.zb);
+    const int z1 = min(a.nz - 1, blockIdx.z * a.zb + a.zb);
+    if (z0 >= z1) return;
+    real tm = __ldg(a.Tin + (long long)(z0 - 1) * a.plane + col);
+    real tc = __ldg(a.Tin + (long long)z0 * a.plane + col);
+    for (int iz = z0; iz < z1; ++iz) {
+        const long long i = (long long)iz * a.plane + col;
+        const real tp = __ldg(a.Tin + i + a.plane);
+        const int m = a.matmap ? a.matmap[i] : (a.plane_mat ? __ldg(a.plane_mat + iz) : 0);
+        const HeatMat<real>& M = a.mat[m];
+        const real q = qin ? __ldg(a.Q + (long long)iz * a.plane + colq) : real(0);   // T:76-77
+        const real sxy = __ldg(a.Tin + i - 1) + __ldg(a.Tin + i + 1) + __ldg(a.Tin + i + a.nx) + __ldg(a.Tin + i - a.nx);
+        // T:85-87 (plus the Pennes term -w dt (T - T_art), zero in the reference)
+        const real tn = tc * M.a0 + M.kxy * sxy + M.kz * (tp + tm) + M.qc * q + M.wTa;
+        a.Tout[i] = tn;
+        if (sizeof(real) == 8) {
+            const double Tc = (double)tn - 273.15;                     // T:88
+            // T:99-102
+            a.TD[i] = a.TD[i] + (Tc < 43.0 ? pow(4.0, Tc - 43.0) : pow(2.0, Tc - 43.0)) * (double)a.dt;
+        } else {
+            const float x = (float)tn + a.T_refm43;                    // T_C - 43
+            const float inc = exp2f(x < 0.0f ? 2.0f * x : x) * (float)a.dt;
+            a.TDf[i] = df_add(a.TDf[i], inc);
+        }
+        tm = tc;
+        tc = tp;
+    }
+}
+
+__global__ void heat_advance_kernel(long long* step_base, int n) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) *step_base += n;
+}
+
+}  // namespace bd
+
+using namespace bd;
+
+extern "C" {
+
+bd_status bd_trajectory_shifts(const bd_trajectory* tr, int32_t* sx, int32_t* sy, int64_t cap, int64_t* n_steps,
+                               int64_t* leg_end, int32_t leg_cap) {
+    return guard([&] {
+        if (!tr || !n_steps) fail(BD_ERR_INVALID_ARG, "null argument");
+        int64_t k = 0;
+        if (tr->kind == BD_TRAJ_SPOTS) {
+            // discrete focal spots: hold shift (spot_sx, spot_sy) for spot_steps steps each
+            if (tr->n_spots <= 0 || !tr->spot_sx || !tr->spot_sy || !tr->spot_steps) fail(BD_ERR_INVALID_ARG, "bad spot list");
+            for (int s = 0; s < tr->n_spots; ++s) {
+                if (tr->spot_steps[s] < 0) fail(BD_ERR_INVALID_ARG, "negative spot duration");
+                for (int64_t n = 0; n < tr->spot_steps[s]; ++n) {
+                    if (sx && k < cap) { sx[k] = tr->spot_sx[s]; sy[k] = tr->spot_sy[s]; }
+                    ++k;
+                }
+                if (leg_end && s < leg_cap) leg_end[s] = k;
+            }
+            *n_steps = k;
+            return;
+        }
+        if (tr->kind != BD_TRAJ_SQUARE_SPIRAL) fail(BD_ERR_INVALID_ARG, "unknown trajectory kind");
+        if (!(tr->speed > 0 && tr->dt > 0 && tr->dxy > 0 && tr->t_acc > 0 && tr->scale > 0) || tr->n_legs < 0)
+            fail(BD_ERR_INVALID_ARG, "bad spiral parameters");
+        // T:141-173 and the loop T:345-410: trapezoidal speed, legs of increase*scale
+        // alternating x / y, position snapped to the nearest grid node.
+        const double dt = tr->dt, dxy = tr->dxy;
+        const int Nt_scale = 1 + (int)(tr->scale / (tr->speed * dt));
+        const int Nt_acc = 1 + (int)(tr->t_acc / dt);
+        const double acc = (tr->speed - tr->speed_init) / tr->t_acc;
+        std::vector<double> speed_acc(Nt_acc);
+        for (int i = 0; i < Nt_acc; i++) speed_acc[i] = tr->speed_init + i * dt * acc;
+        int lines = 0, increase = 1, sign_x = 1, sign_y = -1, shift_x = 0, shift_y = 0;
+        bool right_left = true;
+        double x_s = 0.0, y_s = 0.0, x_next = 0.0, x_prev = 0.0, y_next = 0.0, y_prev = 0.0;
+        double v = tr->speed_init;
+        while (lines < tr->n_legs) {
+            int n = (lines == 0) ? 1 : 0;
+            x_next = x_prev + sign_x * dxy;
+            y_next = y_prev + sign_y * dxy;
+            for (; n < increase * Nt_scale + 2 * Nt_acc; n++) {
+                if (n < Nt_acc) v = speed_acc[n];
+                if (n >= Nt_acc && n < increase * Nt_scale + Nt_acc) v = tr->speed;
+                if (n >= increase * Nt_scale + Nt_acc) v = speed_acc[increase * Nt_scale + 2 * Nt_acc - n - 1];
+                if (right_left) {
+                    x_s = x_s + sign_x * v * dt;
+                    if (std::fabs(x_next - x_s) / dxy < std::fabs(x_s - x_prev) / dxy) {
+                        shift_x += sign_x; x_prev = x_next; x_next = x_next + sign_x * dxy;
+                    }
+                } else {
+                    y_s = y_s + sign_y * v * dt;
+                    if (std::fabs(y_next - y_s) / dxy < std::fabs(y_s - y_prev) / dxy) {
+                        shift_y += sign_y; y_prev = y_next; y_next = y_next + sign_y * dxy;
+                    }
+                }
+                if (sx && k < cap) { sx[k] = shift_x; sy[k] = shift_y; }
+                ++k;
+            }
+            right_left = !right_left;
+            if (right_left) { increase++; sign_x = -sign_x; x_next = x_prev; }
+            else { sign_y = -sign_y; y_next = y_prev; }
+            if (leg_end && lines < leg_cap) leg_end[lines] = k;
+            lines++;
+        }
+        *n_steps = k;
+    });
+}
+
+bd_status bd_spiral_heat_run(bd_context* ctx, const bd_thermal* th, const double* Q, const bd_trajectory* traj,
+                             int64_t max_steps, bd_heat_outputs* out) {
+    return guard([&] {
+        ctx_check(ctx);
+        if (!th || !Q || !traj || !out) fail(BD_ERR_INVALID_ARG, "null argument");
+        const int nx = th->nx, ny = th->ny, nz = th->nz;
+        if (nx < 3 || ny < 3 || nz < 3) fail(BD_ERR_INVALID_ARG, "grid too small");
+        if (th->n_materials < 1 || th->n_materials > BD_MAX_MATERIALS) fail(BD_ERR_INVALID_ARG, "n_materials out of range");
+        if (th->precision != BD_F32 && th->precision != BD_F64) fail(BD_ERR_INVALID_ARG, "bad precision");
+        const bool f64 = th->precision == BD_F64;
+        const long long plane = (long long)nx * ny, n = plane * nz;
+        // trajectory
+        int64_t nsteps = 0;
+        const int leg_cap = 4096;
+        std::vector<int64_t> leg_end(leg_cap, 0);
+        bd_status st = bd_trajectory_shifts(traj, nullptr, nullptr, 0, &nsteps, nullptr, 0);
+        if (st != BD_OK) throw Error{st};
+        std::vector<int32_t> sx(nsteps), sy(nsteps);
+        st = bd_trajectory_shifts(traj, sx.data(), sy.data(), nsteps, &nsteps, leg_end.data(), leg_cap);
+        if (st != BD_OK) throw Error{st};
+        const int n_legs = traj->kind == BD_TRAJ_SPOTS ? traj->n_spots : traj->n_legs;
+        if (max_steps > 0 && max_steps < nsteps) nsteps = max_steps;
+        std::vector<int2> sh(std::max<int64_t>(nsteps, 1));
+        for (int64_t s = 0; s < nsteps; ++s) sh[s] = make_int2(sx[s], sy[s]);
+        // initial fields (T:232-257)
+        auto mat_of = [&](long long i) -> int {
+            int iz = (int)(i / plane);
+            int m = th->material_map ? th->material_map[i] : (th->plane_material ? th->plane_material[iz] : 0);
+            if (m < 0 || m >= th->n_materials) fail(BD_ERR_INVALID_ARG, "material index out of range");
+            return m;
+        };
+        const double T_ref = f64 ? 0.0 : th->T_ref;
+        std::vector<double> T0(n), TD0(n);
+        for (long long i = 0; i < n; ++i) {
+            const bd_thermal_material& mt = th->mat[mat_of(i)];
+            T0[i] = mt.T_init;
+            TD0[i] = th->dose_init ? std::pow(4.0, mt.T_init - 273.15 - 43.0) * th->dt : 0.0;   // T:246, T:252
+        }
+        const size_t esz = f64 ? 8 : 4;
+        PoolBuf Ta, Tb, Qd, TDd, pm, mm, shd, sb;
+        Ta.alloc(ctx, n * esz); Tb.alloc(ctx, n * esz); Qd.alloc(ctx, n * esz);
+        TDd.alloc(ctx, n * 8);
+        shd.alloc(ctx, sh.size() * sizeof(int2));
+        sb.alloc(ctx, 64);
+        BD_CUDA(cudaMemcpy(shd.p, sh.data(), sh.size() * sizeof(int2), cudaMemcpyHostToDevice));
+        if (f64) {
+            BD_CUDA(cudaMemcpy(Ta.p, T0.data(), n * 8, cudaMemcpyHostToDevice));
+            BD_CUDA(cudaMemcpy(Tb.p, T0.data(), n * 8, cudaMemcpyHostToDevice));
+            BD_CUDA(cudaMemcpy(Qd.p, Q, n * 8, cudaMemcpyHostToDevice));
+            BD_CUDA(cudaMemcpy(TDd.p, TD0.data(), n * 8, cudaMemcpyHostToDevice));
+        } else {
+            std::vector<float> tf(n), qf(n);
+            std::vector<float2> df(n);
+            for (long long i = 0; i < n; ++i) {
+                tf[i] = (float)(T0[i] - T_ref);
+                qf[i] = (float)Q[i];
+                const float hi = (float)TD0[i];
+                df[i] = make_float2(hi, (float)(TD0[i] - (double)hi));
+            }
+            BD_CUDA(cudaMemcpy(Ta.p, tf.data(), n * 4, cudaMemcpyHostToDevice));
+            BD_CUDA(cudaMemcpy(Tb.p, tf.data(), n * 4, cudaMemcpyHostToDevice));
+            BD_CUDA(cudaMemcpy(Qd.p, qf.data(), n * 4, cudaMemcpyHostToDevice));
+            BD_CUDA(cudaMemcpy(TDd.p, df.data(), n * 8, cudaMemcpyHostToDevice));
+        }
+        if (th->plane_material) {
+            pm.alloc(ctx, nz * 4);
+            BD_CUDA(cudaMemcpy(pm.p, th->plane_material, nz * 4, cudaMemcpyHostToDevice));
+        }
+        if (th->material_map) {
+            mm.alloc(ctx, n);
+            BD_CUDA(cudaMemcpy(mm.p, th->material_map, n, cudaMemcpyHostToDevice));
+        }
+        BD_CUDA(cudaMemset(sb.p, 0, 64));
+        cudaStream_t s = ctx->stream;
+        const int zb = 32;
+        dim3 block(32, 8), grid((nx + 31) / 32, (ny + 7) / 8, (nz + zb - 1) / zb);
+        // snapshot schedule: after the listed legs (T:412-563)
+        std::vector<std::pair<int64_t, int>> snaps;
+        for (int k = 0; k < out->n_snap; ++k) {
+            const int leg = out->snapshot_legs ? out->snapshot_legs[k] : 0;
+            if (leg < 1 || leg > n_legs || leg > leg_cap) fail(BD_ERR_INVALID_ARG, "snapshot leg %d out of range", leg);
+            snaps.push_back({leg_end[leg - 1], k});
+        }
+        std::sort(snaps.begin(), snaps.end());
+        auto copy_T = [&](const PoolBuf& src, double* dst) {
+            if (f64) {
+                BD_CUDA(cudaMemcpyAsync(dst, src.p, n * 8, cudaMemcpyDeviceToHost, s));
+                BD_CUDA(cudaStreamSynchronize(s));
+            } else {
+                std::vector<float> tf(n);
+                BD_CUDA(cudaMemcpyAsync(tf.data(), src.p, n * 4, cudaMemcpyDeviceToHost, s));
+                BD_CUDA(cudaStreamSynchronize(s));
+                for (long long i = 0; i < n; ++i) dst[i] = T_ref + (double)tf[i];
+            }
+        };
+        auto make_args = [&]() {
+            HeatArgs<float> af;
+            HeatArgs<double> ad;
+            std::memset(&af, 0, sizeof af);
+            std::memset(&ad, 0, sizeof ad);
+            for (int k = 0; k < th->n_materials; ++k) {
+                const bd_thermal_material& mt = th->mat[k];
+                const double kk = mt.k_t / (mt.rho * mt.c_t);
+                const double kxy = th->dt * kk / (th->dx * th->dx), kz = th->dt * kk / (th->dz * th->dz);
+                const double w = mt.perfusion * th->dt;
+                const double a0 = 1.0 - 4.0 * kxy - 2.0 * kz - w;
+                const double qc = th->dt / (mt.rho * mt.c_t);
+                const double wTa = w * (mt.T_art - T_ref);
+                af.mat[k] = HeatMat<float>{(float)a0, (float)kxy, (float)kz, (float)qc, (float)wTa};
+                ad.mat[k] = HeatMat<double>{a0, kxy, kz, qc, wTa};
+            }
+            return std::make_pair(af, ad);
+        };
+        auto margs = make_args();
+        auto fill = [&](auto& a, bool a_to_b, auto tag) {
+            using RR = decltype(tag);
+            a.nx = nx; a.ny = ny; a.nz = nz; a.zb = zb; a.plane = plane;
+            a.Tin = (a_to_b ? Ta : Tb).template as<RR>();
+            a.Tout = (a_to_b ? Tb : Ta).template as<RR>();
+            a.Q = Qd.template as<RR>();
+            a.TD = TDd.template as<double>();
+            a.TDf = TDd.template as<float2>();
+            a.plane_mat = th->plane_material ? pm.template as<int>() : nullptr;
+            a.matmap = th->material_map ? mm.template as<uint8_t>() : nullptr;
+            a.shifts = shd.template as<int2>();
+            a.step_base = sb.template as<long long>();
+            a.dt = (RR)th->dt;
+            a.T_ref = T_ref;
+            a.T_refm43 = (float)(T_ref - 273.15 - 43.0);
+        };
+        BD_CUDA(cudaEventRecord(ctx->ev0, s));
+        int64_t done = 0;
+        size_t isnap = 0;
+        // the reference toggles use_p each step (T:391); with Tin/Tout swapped per
+        // step, after an even number of steps the latest field is Ta
+        auto run_steps = [&](int64_t from, int64_t to) {
+            const int CH = 64;
+            for (int64_t s0 = from; s0 < to; s0 += CH) {
+                const int cnt = (int)std::min<int64_t>(CH, to - s0);
+                for (int k = 0; k < cnt; ++k) {
+                    const bool a_to_b = ((s0 + k) % 2) == 0;
+                    if (f64) {
+                        HeatArgs<double> a = margs.second;
+                        fill(a, a_to_b, 0.0);
+                        heat_step_kernel<double><<<grid, block, 0, s>>>(a, k);
+                    } else {
+                        HeatArgs<float> a = margs.first;
+                        fill(a, a_to_b, 0.0f);
+                        heat_step_kernel<float><<<grid, block, 0, s>>>(a, k);
+                    }
+                    BD_LAUNCHED(ctx);
+                }
+                heat_advance_kernel<<<1, 32, 0, s>>>(sb.as<long long>(), cnt);
+                BD_LAUNCHED(ctx);
+            }
+        };
+        double snap_ms = 0.0;
+        while (done < nsteps) {
+            int64_t next = nsteps;
+            if (isnap < snaps.size()) next = std::min<int64_t>(next, snaps[isnap].first);
+            if (next > done) run_steps(done, next);
+            done = next;
+            while (isnap < snaps.size() && snaps[isnap].first <= done) {
+                if (out->snapshots) {
+                    const PoolBuf& latest = (done % 2 == 0) ? Ta : Tb;
+                    copy_T(latest, static_cast<double*>(out->snapshots) + (size_t)snaps[isnap].second * n);
+                }
+                ++isnap;
+            }
+        }
+        BD_CUDA(cudaEventRecord(ctx->ev1, s));
+        BD_CUDA(cudaEventSynchronize(ctx->ev1));
+        float ms = 0;
+        BD_CUDA(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+        (void)snap_ms;
+        const PoolBuf& latest = (nsteps % 2 == 0) ? Ta : Tb;
+        if (out->T_final) copy_T(latest, static_cast<double*>(out->T_final));
+        if (out->dose) {
+            if (f64) BD_CUDA(cudaMemcpy(out->dose, TDd.p, n * 8, cudaMemcpyDeviceToHost));
+            else {
+                std::vector<float2> df(n);
+                BD_CUDA(cudaMemcpy(df.data(), TDd.p, n * 8, cudaMemcpyDeviceToHost));
+                for (long long i = 0; i < n; ++i) out->dose[i] = (double)df[i].x + (double)df[i].y;
+            }
+        }
+        out->elapsed_ms = ms;
+        out->steps_done = nsteps;
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,816 @@
+// Westervelt solver: host driver behind bd_westervelt_run / _begin / _advance /
+// _finish / checkpoints.  Replaces the host program W:350-790.
+//
+// Device layout (cells x-fastest, W:155):
+//   P[5]          pressure ring; at step s the buffer (4s + k) mod 5 holds p^{s-k}
+//                 and p^{s+1} is written over p^{s-4} (replaces W:575-579)
+//   R[v][2]       relaxation ring; R^n is written over R^{n-2} (replaces W:581-584)
+//   peak, energy  accumulators on every cell; dre/dim DFT planes [n_dft][planes]
+// Steps are issued in chunks of K (a multiple of 10, so that the ring
+// arrangement repeats) captured once as a CUDA graph and replayed; every
+// step-dependent value is read from device tables indexed by a device step
+// counter, so one graph serves every chunk.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "bd_internal.h"
+#include "wv_kernels.cuh"
+
+namespace bd {
+
+struct Variant { int tx, ty, zb; };
+static const Variant kVariants[] = {
+    {32, 8, 32}, {32, 4, 32}, {64, 4, 32}, {32, 8, 64}, {32, 16, 16}, {64, 8, 16}, {128, 2, 32}, {32, 8, 0},
+};
+static const int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
+
+// tuned variant per problem signature (process-wide)
+static std::mutex g_tune_mu;
+static std::map<std::string, int> g_tuned;
+
+struct WvSession {
+    bd_context* ctx = nullptr;
+    bd_grid g{};
+    bd_westervelt_params p{};
+    bd_source s{};
+    int prec = BD_F32;
+    size_t esz = 4;
+    int nx = 0, ny = 0, nz = 0;
+    long long plane = 0, ncell = 0;
+    int max_relax = 0;
+    int n_dft = 0, dz_lo = 0, dz_hi = 0;
+    long long dcells = 0;
+    int64_t step = 0;           // steps done
+    int variant = 0;
+    int chunk = 50;
+    bool any_mur = false;
+    PoolBuf P[5];
+    PoolBuf R[BD_MAX_RELAX][2];
+    PoolBuf peak, energy, dre, dim;
+    PoolBuf cmap, matmap, planemat, wx, wy, wz;
+    PoolBuf sA, sVar, sTau, sAf, sPsi, sTauf, sPhi;
+    PoolBuf t_src, theta, tb0, tw;
+    PoolBuf step_base, flag, kconst, Qd;
+    double tau_max = 0.0;
+    double last_ms = 0.0;
+    cudaGraphExec_t graph = nullptr;
+    int graph_variant = -1;
+    std::vector<bd_material> mats;
+    int n_materials = 0;
+    bool has_cmap = false, has_matmap = false, has_planemat = false;
+
+    ~WvSession() {
+        if (graph) cudaGraphExecDestroy(graph);
+    }
+};
+
+static inline int head_of(int64_t s) { return (int)((4 * (s % 5)) % 5); }
+
+template <class real>
+static WvArgs<real> make_args(WvSession& S, int64_t s) {
+    WvArgs<real> a;
+    std::memset(&a, 0, sizeof a);
+    a.nx = S.nx; a.ny = S.ny; a.nz = S.nz;
+    a.plane = S.plane;
+    const int h = head_of(s);
+    a.p0 = S.P[(h + 0) % 5].as<real>();
+    a.p1 = S.P[(h + 1) % 5].as<real>();
+    a.p2 = S.P[(h + 2) % 5].as<real>();
+    a.p3 = S.P[(h + 3) % 5].as<real>();
+    a.p4 = S.P[(h + 4) % 5].as<real>();
+    const int rh = (int)(s & 1);
+    for (int v = 0; v < S.max_relax; ++v) {
+        a.rcur[v] = S.R[v][rh].as<real>();
+        a.rold[v] = S.R[v][rh ^ 1].as<real>();
+    }
+    a.max_relax = S.max_relax;
+    a.cmap = S.has_cmap ? S.cmap.as<float>() : nullptr;
+    a.matmap = S.has_matmap ? S.matmap.as<uint8_t>() : nullptr;
+    a.plane_mat = S.has_planemat ? S.planemat.as<int>() : nullptr;
+    const bd_grid& g = S.g;
+    a.mir_x = g.face[0] == BD_FACE_MIRROR;
+    a.mir_y = g.face[2] == BD_FACE_MIRROR;
+    a.mur_xp = g.face[1] == BD_FACE_MUR;
+    a.mur_yp = g.face[3] == BD_FACE_MUR;
+    a.mur_zm = g.face[4] == BD_FACE_MUR;
+    a.mur_zp = g.face[5] == BD_FACE_MUR;
+    a.L = g.mur_layers;
+    a.src_iz = (S.s.kind != BD_SRC_NONE) ? S.s.plane_iz : -1;
+    a.Lzm = a.mur_zm ? (a.src_iz >= 0 ? a.src_iz : a.L) : 0;
+    a.xhi = a.mur_xp ? S.nx - 1 - a.L : S.nx - 1;
+    a.yhi = a.mur_yp ? S.ny - 1 - a.L : S.ny - 1;
+    a.zlo = a.Lzm;
+    a.zhi = a.mur_zp ? S.nz - 1 - a.L : S.nz - 1;
+    if (g.sponge_cells > 0) { a.wx = S.wx.as<float>(); a.wy = S.wy.as<float>(); a.wz = S.wz.as<float>(); }
+    a.dt = (real)g.dt;
+    a.kxy180 = (real)(g.dt * g.dt / (g.dx * g.dx) / 180.0);
+    a.kz180 = (real)(g.dt * g.dt / (g.dz * g.dz) / 180.0);
+    a.dt2 = (real)(g.dt * g.dt);
+    a.dtdx = (real)(g.dt / g.dx);
+    a.dtdz = (real)(g.dt / g.dz);
+    a.sA = S.sA.as<double>(); a.sVar = S.sVar.as<double>(); a.sTau = S.sTau.as<double>();
+    a.sPhi = S.sPhi.as<double>();
+    a.sAf = S.sAf.as<float>(); a.sPsi = S.sPsi.as<float>(); a.sTauf = S.sTauf.as<float>();
+    a.n_tones = S.s.n_tones;
+    a.burst = S.s.burst_cycles > 0.0;
+    for (int k = 0; k < BD_MAX_TONES; ++k) {
+        a.freq[k] = S.s.freq[k]; a.tamp[k] = S.s.amp[k]; a.tphase[k] = S.s.phase[k];
+        a.tampf[k] = (float)S.s.amp[k];
+    }
+    a.tau_max = S.tau_max;
+    a.burst_len = a.burst ? S.s.burst_cycles / S.s.freq[0] : 0.0;
+    a.burst_lenf = (float)a.burst_len;
+    a.step_base = S.step_base.as<long long>();
+    a.t_src = S.t_src.as<double>();
+    a.theta = S.theta.as<float>();
+    a.tb0 = S.tb0.as<float>();
+    a.peak = S.peak.as<real>();
+    a.energy = S.energy.as<real>();
+    a.dre = S.dre.as<real>();
+    a.dim = S.dim.as<real>();
+    a.tw = S.tw.as<real>();
+    a.peak_start = S.p.peak_start; a.peak_end = S.p.peak_end;
+    a.energy_start = S.p.energy_start; a.energy_end = S.p.energy_end;
+    a.dft_start = S.p.dft_start; a.dft_len = S.n_dft > 0 ? S.p.dft_len : 0;
+    a.energy_mode = S.p.energy_mode;
+    a.n_dft = S.n_dft; a.dz_lo = S.dz_lo; a.dz_hi = S.dz_hi;
+    a.relax_scheme = S.p.relax_scheme;
+    return a;
+}
+
+template <class real, int TX, int TY>
+static void launch_step_t(WvSession& S, const WvArgs<real>& a, int koff, cudaStream_t st) {
+    dim3 block(TX, TY, 1);
+    dim3 grid((S.nx + TX - 1) / TX, (S.ny + TY - 1) / TY, (S.nz + a.zb - 1) / a.zb);
+    wv_step_kernel<real, TX, TY><<<grid, block, 0, st>>>(a, S.kconst.as<WvConst<real>>(), koff);
+    BD_LAUNCHED(S.ctx);
+}
+
+template <class real>
+static void launch_step(WvSession& S, int variant, int64_t s, int koff, cudaStream_t st) {
+    WvArgs<real> a = make_args<real>(S, s);
+    const Variant& v = kVariants[variant];
+    a.zb = v.zb > 0 ? v.zb : S.nz;
+    switch (variant) {
+        case 0: case 3: case 7: launch_step_t<real, 32, 8>(S, a, koff, st); break;
+        case 1: launch_step_t<real, 32, 4>(S, a, koff, st); break;
+        case 2: launch_step_t<real, 64, 4>(S, a, koff, st); break;
+        case 4: launch_step_t<real, 32, 16>(S, a, koff, st); break;
+        case 5: launch_step_t<real, 64, 8>(S, a, koff, st); break;
+        case 6: launch_step_t<real, 128, 2>(S, a, koff, st); break;
+        default: fail(BD_ERR_INVALID_ARG, "bad tile variant %d", variant);
+    }
+    if (S.any_mur) {
+        const WvConst<real>* K = S.kconst.as<WvConst<real>>();
+        if (a.mur_zm || a.mur_zp) {
+            dim3 b(32, 8), gr((S.nx + 31) / 32, (S.ny + 7) / 8);
+            wv_mur_z_kernel<real><<<gr, b, 0, st>>>(a, K, koff);
+            BD_LAUNCHED(S.ctx);
+        }
+        if (a.mur_xp) {
+            dim3 b(128), gr((S.ny + 127) / 128, S.nz);
+            wv_mur_x_kernel<real><<<gr, b, 0, st>>>(a, K, koff);
+            BD_LAUNCHED(S.ctx);
+        }
+        if (a.mur_yp) {
+            dim3 b(128), gr((S.nx + 127) / 128, S.nz);
+            wv_mur_y_kernel<real><<<gr, b, 0, st>>>(a, K, koff);
+            BD_LAUNCHED(S.ctx);
+        }
+    }
+}
+
+// Issue steps [s, s+n) on the stream (no graph): kernels read *step_base + koff,
+// then one advance kernel moves the counter by n.
+static void issue_steps(WvSession& S, int variant, int64_t s, int n, cudaStream_t st) {
+    for (int k = 0; k < n; ++k) {
+        if (S.prec == BD_F32) launch_step<float>(S, variant, s + k, k, st);
+        else launch_step<double>(S, variant, s + k, k, st);
+    }
+    wv_advance_kernel<<<1, 32, 0, st>>>(S.step_base.as<long long>(), n);
+    BD_LAUNCHED(S.ctx);
+}
+
+static void build_graph(WvSession& S) {
+    if (S.graph) { cudaGraphExecDestroy(S.graph); S.graph = nullptr; }
+    cudaStream_t cs;
+    BD_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    cudaGraph_t g = nullptr;
+    const int64_t launches_before = S.ctx->launches;
+    BD_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+    try {
+        issue_steps(S, S.variant, 0, S.chunk, cs);   // base arrangement: chunk starts at s = 0 mod 10
+    } catch (...) {
+        cudaStreamEndCapture(cs, &g);
+        if (g) cudaGraphDestroy(g);
+        cudaStreamDestroy(cs);
+        throw;
+    }
+    BD_CUDA(cudaStreamEndCapture(cs, &g));
+    S.ctx->launches = launches_before;   // captured, not yet launched
+    BD_CUDA(cudaGraphInstantiate(&S.graph, g, 0));
+    cudaGraphDestroy(g);
+    cudaStreamDestroy(cs);
+    S.graph_variant = S.variant;
+}
+
+static int64_t launches_per_step(const WvSession& S) {
+    int64_t n = 1;
+    if (S.any_mur) {
+        if (S.g.face[4] == BD_FACE_MUR || S.g.face[5] == BD_FACE_MUR) n++;
+        if (S.g.face[1] == BD_FACE_MUR) n++;
+        if (S.g.face[3] == BD_FACE_MUR) n++;
+    }
+    return n;
+}
+
+static void probe(WvSession& S) {
+    unsigned* f = S.flag.as<unsigned>();
+    BD_CUDA(cudaMemsetAsync(f, 0, sizeof(unsigned), S.ctx->stream));
+    const int h = head_of(S.step);
+    if (S.prec == BD_F32)
+        wv_probe_kernel<float><<<S.ctx->sm_count * 4, 256, 0, S.ctx->stream>>>(S.P[h].as<float>(), S.ncell, S.p.blowup_limit, f);
+    else
+        wv_probe_kernel<double><<<S.ctx->sm_count * 4, 256, 0, S.ctx->stream>>>(S.P[h].as<double>(), S.ncell, S.p.blowup_limit, f);
+    BD_LAUNCHED(S.ctx);
+    unsigned hf = 0;
+    BD_CUDA(cudaMemcpyAsync(&hf, f, sizeof hf, cudaMemcpyDeviceToHost, S.ctx->stream));
+    BD_CUDA(cudaStreamSynchronize(S.ctx->stream));
+    if (hf & 1u) fail(BD_ERR_UNSTABLE, "non-finite pressure after step %lld", (long long)S.step);
+    if (hf & 2u) fail(BD_ERR_UNSTABLE, "|p| above %g after step %lld", S.p.blowup_limit, (long long)S.step);
+}
+
+// Advance n steps from the current step, with graph replays for whole chunks.
+static void advance(WvSession& S, int64_t n, bool use_graph) {
+    cudaStream_t st = S.ctx->stream;
+    int64_t end = S.step + n;
+    const int64_t fault = S.p.fault_at_step;
+    bool faulted = false;
+    if (fault >= 0 && fault >= S.step && fault < end) { end = fault; faulted = true; }
+    const int64_t per = launches_per_step(S) + 0;
+    int64_t next_probe = S.p.check_every > 0 ? ((S.step / S.p.check_every) + 1) * S.p.check_every : INT64_MAX;
+    while (S.step < end) {
+        int64_t todo = end - S.step;
+        const int64_t to_align = (S.chunk - (S.step % S.chunk)) % S.chunk;
+        int64_t take;
+        if (use_graph && to_align == 0 && todo >= S.chunk) {
+            if (!S.graph || S.graph_variant != S.variant) build_graph(S);
+            BD_CUDA(cudaGraphLaunch(S.graph, st));
+            S.ctx->launches += per * S.chunk + 1;
+            take = S.chunk;
+        } else {
+            take = std::min<int64_t>(todo, to_align > 0 ? to_align : S.chunk);
+            issue_steps(S, S.variant, S.step, (int)take, st);
+        }
+        S.step += take;
+        if (S.step >= next_probe) {
+            probe(S);
+            next_probe = ((S.step / S.p.check_every) + 1) * S.p.check_every;
+        }
+    }
+    if (faulted) {
+        BD_CUDA(cudaStreamSynchronize(st));
+        fail(BD_ERR_FAULT_INJECTED, "fault injected before step %lld", (long long)fault);
+    }
+}
+
+static void zero_state(WvSession& S) {
+    cudaStream_t st = S.ctx->stream;
+    for (auto& b : S.P) BD_CUDA(cudaMemsetAsync(b.p, 0, b.bytes, st));
+    for (int v = 0; v < S.max_relax; ++v)
+        for (auto& b : S.R[v]) BD_CUDA(cudaMemsetAsync(b.p, 0, b.bytes, st));
+    BD_CUDA(cudaMemsetAsync(S.peak.p, 0, S.peak.bytes, st));
+    BD_CUDA(cudaMemsetAsync(S.energy.p, 0, S.energy.bytes, st));
+    if (S.dre.p) { BD_CUDA(cudaMemsetAsync(S.dre.p, 0, S.dre.bytes, st)); BD_CUDA(cudaMemsetAsync(S.dim.p, 0, S.dim.bytes, st)); }
+    BD_CUDA(cudaMemsetAsync(S.step_base.p, 0, sizeof(long long), st));
+    S.step = 0;
+}
+
+static std::string tune_key(const WvSession& S) {
+    char b[256];
+    snprintf(b, sizeof b, "%d:%d:%d:%d:%d:%d:%d:%d", S.nx, S.ny, S.nz, S.prec, S.max_relax, S.has_cmap ? 1 : 0,
+             S.any_mur ? 1 : 0, S.n_dft);
+    return b;
+}
+
+// Pick the fastest tile variant: a few steps of each on the (zero) initial
+// state, timed with events, then the state is cleared again.
+static void autotune(WvSession& S) {
+    const std::string key = tune_key(S);
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tuned.find(key);
+        if (it != g_tuned.end()) { S.variant = it->second; return; }
+    }
+    cudaStream_t st = S.ctx->stream;
+    float best = 1e30f;
+    int best_v = 0;
+    const int reps = 4;
+    for (int v = 0; v < kNumVariants; ++v) {
+        if (kVariants[v].zb == 0 && S.nz > 512) continue;
+        issue_steps(S, v, S.step, 2, st);  // warm-up
+        S.step += 2;
+        BD_CUDA(cudaEventRecord(S.ctx->ev0, st));
+        issue_steps(S, v, S.step, reps, st);
+        S.step += reps;
+        BD_CUDA(cudaEventRecord(S.ctx->ev1, st));
+        BD_CUDA(cudaEventSynchronize(S.ctx->ev1));
+        float ms = 0;
+        BD_CUDA(cudaEventElapsedTime(&ms, S.ctx->ev0, S.ctx->ev1));
+        if (ms < best) { best = ms; best_v = v; }
+    }
+    zero_state(S);
+    BD_CUDA(cudaStreamSynchronize(st));
+    S.variant = best_v;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tuned[key] = best_v;
+}
+
+template <class real>
+static void upload_consts(WvSession& S, const bd_medium* m) {
+    WvConst<real> K;
+    std::memset(&K, 0, sizeof K);
+    const double dt = S.g.dt;
+    for (int k = 0; k < m->n_materials; ++k) {
+        const bd_material& mt = m->mat[k];
+        MatConst<real>& M = K.mat[k];
+        M.c0 = (real)mt.c0;
+        M.delta_2dt = (real)(mt.delta / (2.0 * dt));
+        M.beta2_rho = (real)(2.0 * mt.beta / mt.rho);
+        M.n_relax = mt.n_relax;
+        for (int v = 0; v < mt.n_relax; ++v) {
+            const double tau = mt.relax_tau[v], cv = mt.relax_c[v];
+            M.ra_num[v] = (real)((2.0 * dt * 2.0 * cv * tau) / (2.0 * dt * dt * dt) / (2.0 * dt + 3.0 * tau));
+            M.rb[v] = (real)(tau / (2.0 * dt + 3.0 * tau));
+        }
+    }
+    S.kconst.alloc(S.ctx, sizeof K);
+    BD_CUDA(cudaMemcpy(S.kconst.p, &K, sizeof K, cudaMemcpyHostToDevice));
+}
+
+template <class T>
+static void upload(WvSession& S, PoolBuf& b, const std::vector<T>& v) {
+    b.alloc(S.ctx, v.size() * sizeof(T));
+    if (!v.empty()) BD_CUDA(cudaMemcpy(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+}
+
+static double frac(double x) { return x - std::floor(x); }
+
+static void setup(WvSession& S, bd_context* ctx, const bd_grid* g, const bd_medium* m, const bd_source* src,
+                  const bd_westervelt_params* p) {
+    if (!ctx || !g || !m || !p) fail(BD_ERR_INVALID_ARG, "null argument");
+    S.ctx = ctx;
+    S.g = *g;
+    S.p = *p;
+    if (src) S.s = *src;
+    else { std::memset(&S.s, 0, sizeof S.s); S.s.kind = BD_SRC_NONE; }
+    S.prec = p->precision;
+    if (S.prec != BD_F32 && S.prec != BD_F64) fail(BD_ERR_INVALID_ARG, "precision must be BD_F32 or BD_F64");
+    S.esz = S.prec == BD_F32 ? 4 : 8;
+    S.nx = g->nx; S.ny = g->ny; S.nz = g->nz;
+    if (S.nx < 8 || S.ny < 8 || S.nz < 8) fail(BD_ERR_INVALID_ARG, "grid must be at least 8 cells per axis");
+    if (!(g->dt > 0 && g->dx > 0 && g->dz > 0)) fail(BD_ERR_INVALID_ARG, "dt, dx, dz must be positive");
+    if (g->face[0] == BD_FACE_MUR || g->face[2] == BD_FACE_MUR)
+        fail(BD_ERR_UNSUPPORTED, "Mur on the x-/y- faces is not supported (the reference mirrors them)");
+    if (g->face[1] == BD_FACE_MIRROR || g->face[3] == BD_FACE_MIRROR || g->face[4] == BD_FACE_MIRROR ||
+        g->face[5] == BD_FACE_MIRROR)
+        fail(BD_ERR_INVALID_ARG, "mirror planes exist only at x = 0 and y = 0");
+    S.any_mur = false;
+    for (int f = 0; f < 6; ++f) if (g->face[f] == BD_FACE_MUR) S.any_mur = true;
+    if (S.any_mur && (g->mur_layers < 1 || g->mur_layers > 8)) fail(BD_ERR_INVALID_ARG, "mur_layers must be 1..8");
+    if (m->n_materials < 1 || m->n_materials > BD_MAX_MATERIALS) fail(BD_ERR_INVALID_ARG, "n_materials out of range");
+    S.plane = (long long)S.nx * S.ny;
+    S.ncell = S.plane * S.nz;
+    S.max_relax = 0;
+    for (int k = 0; k < m->n_materials; ++k) {
+        if (m->mat[k].n_relax < 0 || m->mat[k].n_relax > BD_MAX_RELAX) fail(BD_ERR_INVALID_ARG, "n_relax out of range");
+        if (!(m->mat[k].c0 > 0 || m->c_map)) fail(BD_ERR_INVALID_ARG, "material %d has no sound speed", k);
+        if (!(m->mat[k].rho > 0)) fail(BD_ERR_INVALID_ARG, "material %d density must be positive", k);
+        S.max_relax = std::max(S.max_relax, m->mat[k].n_relax);
+    }
+    if (S.s.kind != BD_SRC_NONE) {
+        if (S.s.plane_iz < 0 || S.s.plane_iz >= S.nz) fail(BD_ERR_INVALID_ARG, "source plane outside the grid");
+        if (S.s.n_tones < 1 || S.s.n_tones > BD_MAX_TONES) fail(BD_ERR_INVALID_ARG, "n_tones out of range");
+        if (S.s.focal_length <= 0 || S.s.c_delay <= 0) fail(BD_ERR_INVALID_ARG, "bad source geometry");
+        if (S.s.kind == BD_SRC_ARRAY && (!S.s.element_of_cell || S.s.n_elements <= 0))
+            fail(BD_ERR_INVALID_ARG, "array source needs element_of_cell and n_elements");
+    }
+    if (p->n_steps < 0) fail(BD_ERR_INVALID_ARG, "n_steps < 0");
+    if (p->relax_scheme != BD_RELAX_REFERENCE && p->relax_scheme != BD_RELAX_SEMI_IMPLICIT)
+        fail(BD_ERR_INVALID_ARG, "unknown relax_scheme");
+    S.n_dft = p->n_dft;
+    if (S.n_dft < 0 || S.n_dft > BD_MAX_DFT) fail(BD_ERR_INVALID_ARG, "n_dft out of range");
+    if (S.n_dft > 0) {
+        S.dz_lo = std::max(0, p->dft_z_lo);
+        S.dz_hi = std::min(S.nz, p->dft_z_hi);
+        if (S.dz_hi <= S.dz_lo || p->dft_len <= 0) S.n_dft = 0;
+    }
+    S.dcells = S.n_dft > 0 ? (long long)(S.dz_hi - S.dz_lo) * S.plane : 0;
+    S.chunk = p->graph_chunk > 0 ? ((p->graph_chunk + 9) / 10) * 10 : 50;
+
+    BD_CUDA(cudaSetDevice(ctx->device));
+    // state
+    for (auto& b : S.P) b.alloc(ctx, S.ncell * S.esz);
+    for (int v = 0; v < S.max_relax; ++v)
+        for (auto& b : S.R[v]) b.alloc(ctx, S.ncell * S.esz);
+    S.peak.alloc(ctx, S.ncell * S.esz);
+    S.energy.alloc(ctx, S.ncell * S.esz);
+    if (S.n_dft > 0) {
+        S.dre.alloc(ctx, (size_t)S.n_dft * S.dcells * S.esz);
+        S.dim.alloc(ctx, (size_t)S.n_dft * S.dcells * S.esz);
+    }
+    S.step_base.alloc(ctx, 64);
+    S.flag.alloc(ctx, 64);
+    // medium
+    S.has_cmap = m->c_map != nullptr;
+    S.has_matmap = m->material_map != nullptr;
+    S.has_planemat = m->plane_material != nullptr;
+    if (S.has_cmap) {
+        S.cmap.alloc(ctx, S.ncell * 4);
+        BD_CUDA(cudaMemcpy(S.cmap.p, m->c_map, S.ncell * 4, cudaMemcpyHostToDevice));
+    }
+    if (S.has_matmap) {
+        for (long long i = 0; i < S.ncell; ++i)
+            if (m->material_map[i] >= m->n_materials) fail(BD_ERR_INVALID_ARG, "material_map entry out of range");
+        S.matmap.alloc(ctx, S.ncell);
+        BD_CUDA(cudaMemcpy(S.matmap.p, m->material_map, S.ncell, cudaMemcpyHostToDevice));
+    }
+    if (S.has_planemat) {
+        for (int iz = 0; iz < S.nz; ++iz)
+            if (m->plane_material[iz] < 0 || m->plane_material[iz] >= m->n_materials)
+                fail(BD_ERR_INVALID_ARG, "plane_material entry out of range");
+        S.planemat.alloc(ctx, S.nz * 4);
+        BD_CUDA(cudaMemcpy(S.planemat.p, m->plane_material, S.nz * 4, cudaMemcpyHostToDevice));
+    }
+    S.n_materials = m->n_materials;
+    S.mats.assign(m->mat, m->mat + m->n_materials);
+    if (S.prec == BD_F32) upload_consts<float>(S, m);
+    else upload_consts<double>(S, m);
+    // sponge profiles w(d) = exp(-strength (d/W)^2) on OPEN faces
+    {
+        auto prof = [&](int n, int lo, int hi) {
+            std::vector<float> w(n, 1.0f);
+            const int W = g->sponge_cells;
+            for (int i = 0; i < n && W > 0; ++i) {
+                double f = 1.0;
+                if (lo == BD_FACE_OPEN && i < W) { double d = (double)(W - i) / W; f *= std::exp(-g->sponge_strength * d * d); }
+                if (hi == BD_FACE_OPEN && i >= n - W) { double d = (double)(i - (n - W) + 1) / W; f *= std::exp(-g->sponge_strength * d * d); }
+                w[i] = (float)f;
+            }
+            return w;
+        };
+        if (g->sponge_cells > 0) {
+            upload(S, S.wx, prof(S.nx, g->face[0], g->face[1]));
+            upload(S, S.wy, prof(S.ny, g->face[2], g->face[3]));
+            upload(S, S.wz, prof(S.nz, g->face[4], g->face[5]));
+        }
+    }
+    // source plane (W:62-85): amplitude, var, delay per plane cell
+    const long long np = S.plane;
+    std::vector<double> A(np, 0.0), var(np, 1.0), tau(np, 0.0), phi(np, 0.0);
+    S.tau_max = 0.0;
+    if (S.s.kind != BD_SRC_NONE) {
+        const double d = S.s.focal_length;
+        for (int iy = 0; iy < S.ny; ++iy)
+            for (int ix = 0; ix < S.nx; ++ix) {
+                const long long j = (long long)iy * S.nx + ix;
+                const double X = g->x0 + ix * g->dx - S.s.cx;
+                const double Y = g->y0 + iy * g->dx - S.s.cy;
+                const double r = std::sqrt(X * X + Y * Y);
+                if (r <= d * std::tan(S.s.alpha) && r >= d * std::tan(S.s.alpha_hole)) {
+                    const double vr = std::sqrt(1.0 + std::pow(r / d, 2));
+                    double amp = S.s.p0, ph = 0.0;
+                    if (S.s.kind == BD_SRC_ARRAY) {
+                        const int e = S.s.element_of_cell[j];
+                        if (e < 0 || e >= S.s.n_elements) continue;
+                        amp *= S.s.element_amp ? S.s.element_amp[e] : 1.0;
+                        ph = S.s.element_phase ? S.s.element_phase[e] : 0.0;
+                    }
+                    A[j] = amp; var[j] = vr; tau[j] = d * (vr - 1.0) / S.s.c_delay; phi[j] = ph;
+                    S.tau_max = std::max(S.tau_max, tau[j]);
+                }
+            }
+    }
+    const bool burst = S.s.kind != BD_SRC_NONE && S.s.burst_cycles > 0.0;
+    if (S.prec == BD_F64) {
+        upload(S, S.sA, A); upload(S, S.sVar, var); upload(S, S.sTau, tau); upload(S, S.sPhi, phi);
+    } else {
+        std::vector<float> Af(np), psi((size_t)BD_MAX_TONES * np, 0.0f), tauf(np);
+        for (long long j = 0; j < np; ++j) {
+            Af[j] = (float)(A[j] / var[j]);
+            tauf[j] = (float)tau[j];
+            for (int k = 0; k < S.s.n_tones && k < BD_MAX_TONES; ++k) {
+                // 2 pi frac(f tau) + phase_k + element phase, reduced to [0, 2 pi)
+                const double ang = 2.0 * BD_PI * frac(S.s.freq[k] * tau[j]) + S.s.phase[k] + phi[j];
+                psi[(size_t)k * np + j] = (float)(ang - 2.0 * BD_PI * std::floor(ang / (2.0 * BD_PI)));
+            }
+        }
+        upload(S, S.sAf, Af); upload(S, S.sPsi, psi); upload(S, S.sTauf, tauf);
+    }
+    // per-step tables
+    const int64_t N = std::max<int64_t>(p->n_steps, 1);
+    std::vector<double> ts(N);
+    for (int64_t s = 0; s < N; ++s) ts[s] = p->t_src ? p->t_src[s] : p->t0 + (double)(s + 1) * g->dt;
+    upload(S, S.t_src, ts);
+    if (S.prec == BD_F32) {
+        std::vector<float> th((size_t)N * BD_MAX_TONES, 0.0f), tb(N, 0.0f);
+        for (int64_t s = 0; s < N; ++s) {
+            const double tshift = burst ? ts[s] - S.tau_max : ts[s];
+            tb[s] = (float)(ts[s] - S.tau_max);
+            for (int k = 0; k < S.s.n_tones && k < BD_MAX_TONES; ++k)
+                th[(size_t)s * BD_MAX_TONES + k] = (float)(2.0 * BD_PI * frac(S.s.freq[k] * tshift));
+        }
+        upload(S, S.theta, th); upload(S, S.tb0, tb);
+    }
+    if (S.n_dft > 0) {
+        const int64_t L = p->dft_len;
+        std::vector<double> twd((size_t)L * S.n_dft * 2);
+        for (int64_t s = 0; s < L; ++s)
+            for (int j = 0; j < S.n_dft; ++j) {
+                const double th = 2.0 * BD_PI * p->dft_freq[j] * ((double)s * g->dt);
+                twd[((size_t)s * S.n_dft + j) * 2] = std::cos(th);
+                twd[((size_t)s * S.n_dft + j) * 2 + 1] = std::sin(th);
+            }
+        if (S.prec == BD_F64) upload(S, S.tw, twd);
+        else {
+            std::vector<float> twf(twd.begin(), twd.end());
+            upload(S, S.tw, twf);
+        }
+    }
+    zero_state(S);
+    BD_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (p->tile_variant >= 0) {
+        if (p->tile_variant >= kNumVariants) fail(BD_ERR_INVALID_ARG, "tile_variant out of range");
+        S.variant = p->tile_variant;
+    } else if (S.ncell >= (1LL << 21) && p->n_steps >= 200) {
+        autotune(S);
+    } else {
+        S.variant = 0;
+    }
+}
+
+// Acoustic power of W:242-265 (water planes) and W:324-345 (harmonics), in double.
+template <class real>
+__global__ void wv_q_kernel(const real* __restrict__ energy, const real* __restrict__ dre, const real* __restrict__ dim,
+                            const float* __restrict__ cmap, const uint8_t* __restrict__ matmap,
+                            const int* __restrict__ planemat, const bd_material* __restrict__ mats, int nx, int ny,
+                            int nz, int split, int n_harm, int n_dft, int dz_lo, int dz_hi, double f, double dft_len,
+                            double* __restrict__ Q) {
+    const long long plane = (long long)nx * ny;
+    const long long n = plane * nz;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const int iz = (int)(i / plane);
+        const int m = matmap ? matmap[i] : (planemat ? planemat[iz] : 0);
+        const bd_material& mt = mats[m];
+        const double c = cmap ? (double)cmap[i] : mt.c0;
+        double q = 0.0;
+        if (iz >= split) {
+            if (iz >= dz_lo && iz < dz_hi) {
+                const long long pl = (long long)(iz - dz_lo) * plane + (i % plane);
+                const long long stride = (long long)(dz_hi - dz_lo) * plane;
+                for (int h = 1; h <= n_harm && h <= n_dft; ++h) {
+                    const double re = (double)dre[(h - 1) * stride + pl], im = (double)dim[(h - 1) * stride + pl];
+                    const double a = sqrt(re * re + im * im) / dft_len;               // W:299
+                    const double In = 2.0 * a * a / (mt.rho * c);                     // W:341
+                    q = q + (2.0 * (mt.harm_absorption * h * f / 1e6) * In);          // W:342
+                }
+            }
+        } else {
+            q = 2.0 * mt.absorption * f * (double)energy[i] / ((2.0 * BD_PI * f) * (2.0 * BD_PI * f) * mt.rho * c);  // W:261
+        }
+        Q[i] = q;
+    }
+}
+
+static void finish(WvSession& S, bd_westervelt_outputs* o) {
+    cudaStream_t st = S.ctx->stream;
+    BD_CUDA(cudaStreamSynchronize(st));
+    const size_t bytes = S.ncell * S.esz;
+    const int h = head_of(S.step);
+    if (o->p_final) BD_CUDA(cudaMemcpy(o->p_final, S.P[h].p, bytes, cudaMemcpyDeviceToHost));
+    if (o->peak) BD_CUDA(cudaMemcpy(o->peak, S.peak.p, bytes, cudaMemcpyDeviceToHost));
+    if (o->energy) BD_CUDA(cudaMemcpy(o->energy, S.energy.p, bytes, cudaMemcpyDeviceToHost));
+    if (S.n_dft > 0 && o->dft_re) BD_CUDA(cudaMemcpy(o->dft_re, S.dre.p, S.dre.bytes, cudaMemcpyDeviceToHost));
+    if (S.n_dft > 0 && o->dft_im) BD_CUDA(cudaMemcpy(o->dft_im, S.dim.p, S.dim.bytes, cudaMemcpyDeviceToHost));
+    if (o->Q && S.p.q_mode == BD_Q_REFERENCE) {
+        S.Qd.alloc(S.ctx, S.ncell * 8);
+        PoolBuf mats;
+        upload(S, mats, S.mats);
+        const int blocks = S.ctx->sm_count * 8;
+        if (S.prec == BD_F32)
+            wv_q_kernel<float><<<blocks, 256, 0, st>>>(S.energy.as<float>(), S.dre.as<float>(), S.dim.as<float>(),
+                                                       S.has_cmap ? S.cmap.as<float>() : nullptr,
+                                                       S.has_matmap ? S.matmap.as<uint8_t>() : nullptr,
+                                                       S.has_planemat ? S.planemat.as<int>() : nullptr,
+                                                       mats.as<bd_material>(), S.nx, S.ny, S.nz, S.p.q_iz_split,
+                                                       S.p.q_n_harm, S.n_dft, S.dz_lo, S.dz_hi, S.p.q_freq,
+                                                       (double)S.p.dft_len, S.Qd.as<double>());
+        else
+            wv_q_kernel<double><<<blocks, 256, 0, st>>>(S.energy.as<double>(), S.dre.as<double>(), S.dim.as<double>(),
+                                                        S.has_cmap ? S.cmap.as<float>() : nullptr,
+                                                        S.has_matmap ? S.matmap.as<uint8_t>() : nullptr,
+                                                        S.has_planemat ? S.planemat.as<int>() : nullptr,
+                                                        mats.as<bd_material>(), S.nx, S.ny, S.nz, S.p.q_iz_split,
+                                                        S.p.q_n_harm, S.n_dft, S.dz_lo, S.dz_hi, S.p.q_freq,
+                                                        (double)S.p.dft_len, S.Qd.as<double>());
+        BD_LAUNCHED(S.ctx);
+        BD_CUDA(cudaMemcpyAsync(o->Q, S.Qd.p, S.ncell * 8, cudaMemcpyDeviceToHost, st));
+        BD_CUDA(cudaStreamSynchronize(st));
+    }
+    o->steps_done = S.step;
+}
+
+// ---------------------------------------------------------------- checkpoint
+struct CkHeader {
+    char magic[8];
+    int32_t version, precision, nx, ny, nz, max_relax, n_dft, pad;
+    int64_t step, dcells;
+};
+
+static size_t ck_size(const WvSession& S) {
+    const size_t f = S.ncell * S.esz;
+    return sizeof(CkHeader) + f * (5 + 2 * (size_t)S.max_relax + 2) + 2 * (size_t)S.n_dft * S.dcells * S.esz;
+}
+
+static void ck_save(WvSession& S, void* blob, size_t bytes) {
+    if (bytes < ck_size(S)) fail(BD_ERR_INVALID_ARG, "checkpoint buffer too small (%zu < %zu)", bytes, ck_size(S));
+    BD_CUDA(cudaStreamSynchronize(S.ctx->stream));
+    CkHeader h;
+    std::memset(&h, 0, sizeof h);
+    std::memcpy(h.magic, "BDCKPT01", 8);
+    h.version = 1; h.precision = S.prec; h.nx = S.nx; h.ny = S.ny; h.nz = S.nz;
+    h.max_relax = S.max_relax; h.n_dft = S.n_dft; h.step = S.step; h.dcells = S.dcells;
+    char* o = static_cast<char*>(blob);
+    std::memcpy(o, &h, sizeof h);
+    o += sizeof h;
+    const size_t f = S.ncell * S.esz;
+    const int hd = head_of(S.step);
+    for (int k = 0; k < 5; ++k) { BD_CUDA(cudaMemcpy(o, S.P[(hd + k) % 5].p, f, cudaMemcpyDeviceToHost)); o += f; }
+    const int rh = (int)(S.step & 1);
+    for (int v = 0; v < S.max_relax; ++v)
+        for (int k = 0; k < 2; ++k) { BD_CUDA(cudaMemcpy(o, S.R[v][rh ^ k].p, f, cudaMemcpyDeviceToHost)); o += f; }
+    BD_CUDA(cudaMemcpy(o, S.peak.p, f, cudaMemcpyDeviceToHost)); o += f;
+    BD_CUDA(cudaMemcpy(o, S.energy.p, f, cudaMemcpyDeviceToHost)); o += f;
+    if (S.n_dft > 0) {
+        BD_CUDA(cudaMemcpy(o, S.dre.p, S.dre.bytes, cudaMemcpyDeviceToHost)); o += S.dre.bytes;
+        BD_CUDA(cudaMemcpy(o, S.dim.p, S.dim.bytes, cudaMemcpyDeviceToHost)); o += S.dim.bytes;
+    }
+}
+
+static void ck_load(WvSession& S, const void* blob, size_t bytes) {
+    if (bytes < sizeof(CkHeader)) fail(BD_ERR_INVALID_ARG, "checkpoint too small");
+    CkHeader h;
+    std::memcpy(&h, blob, sizeof h);
+    if (std::memcmp(h.magic, "BDCKPT01", 8) != 0) fail(BD_ERR_INVALID_ARG, "not a checkpoint blob");
+    if (h.precision != S.prec || h.nx != S.nx || h.ny != S.ny || h.nz != S.nz || h.max_relax != S.max_relax ||
+        h.n_dft != S.n_dft || h.dcells != S.dcells)
+        fail(BD_ERR_STATE, "checkpoint geometry does not match this solve");
+    if (bytes < ck_size(S)) fail(BD_ERR_INVALID_ARG, "checkpoint truncated");
+    const char* in = static_cast<const char*>(blob) + sizeof h;
+    const size_t f = S.ncell * S.esz;
+    BD_CUDA(cudaStreamSynchronize(S.ctx->stream));
+    const int hd = head_of(h.step);
+    for (int k = 0; k < 5; ++k) { BD_CUDA(cudaMemcpy(S.P[(hd + k) % 5].p, in, f, cudaMemcpyHostToDevice)); in += f; }
+    const int rh = (int)(h.step & 1);
+    for (int v = 0; v < S.max_relax; ++v)
+        for (int k = 0; k < 2; ++k) { BD_CUDA(cudaMemcpy(S.R[v][rh ^ k].p, in, f, cudaMemcpyHostToDevice)); in += f; }
+    BD_CUDA(cudaMemcpy(S.peak.p, in, f, cudaMemcpyHostToDevice)); in += f;
+    BD_CUDA(cudaMemcpy(S.energy.p, in, f, cudaMemcpyHostToDevice)); in += f;
+    if (S.n_dft > 0) {
+        BD_CUDA(cudaMemcpy(S.dre.p, in, S.dre.bytes, cudaMemcpyHostToDevice)); in += S.dre.bytes;
+        BD_CUDA(cudaMemcpy(S.dim.p, in, S.dim.bytes, cudaMemcpyHostToDevice)); in += S.dim.bytes;
+    }
+    long long st = h.step;
+    BD_CUDA(cudaMemcpy(S.step_base.p, &st, sizeof st, cudaMemcpyHostToDevice));
+    S.step = h.step;
+}
+
+}  // namespace bd
+
+struct bd_westervelt {
+    bd::WvSession S;
+};
+
+using namespace bd;
+
+static double timed_advance(WvSession& S, int64_t n) {
+    BD_CUDA(cudaEventRecord(S.ctx->ev0, S.ctx->stream));
+    bool graph = S.p.graph_chunk >= 0;
+    advance(S, n, graph);
+    BD_CUDA(cudaEventRecord(S.ctx->ev1, S.ctx->stream));
+    BD_CUDA(cudaEventSynchronize(S.ctx->ev1));
+    float ms = 0;
+    BD_CUDA(cudaEventElapsedTime(&ms, S.ctx->ev0, S.ctx->ev1));
+    S.last_ms = ms;
+    return ms;
+}
+
+extern "C" {
+
+bd_status bd_westervelt_begin(bd_context* ctx, const bd_grid* grid, const bd_medium* medium, const bd_source* source,
+                              const bd_westervelt_params* params, bd_westervelt** out) {
+    return guard([&] {
+        if (!out) fail(BD_ERR_INVALID_ARG, "null output");
+        *out = nullptr;
+        ctx_check(ctx);
+        auto* w = new bd_westervelt();
+        try {
+            setup(w->S, ctx, grid, medium, source, params);
+        } catch (...) {
+            delete w;
+            throw;
+        }
+        *out = w;
+    });
+}
+
+bd_status bd_westervelt_advance(bd_westervelt* w, int64_t n_steps) {
+    return guard([&] {
+        if (!w) fail(BD_ERR_INVALID_ARG, "null session");
+        ctx_check(w->S.ctx);
+        if (n_steps < 0) fail(BD_ERR_INVALID_ARG, "negative step count");
+        if (w->S.step + n_steps > w->S.p.n_steps)
+            fail(BD_ERR_INVALID_ARG, "advance past n_steps (%lld + %lld > %lld)", (long long)w->S.step,
+                 (long long)n_steps, (long long)w->S.p.n_steps);
+        timed_advance(w->S, n_steps);
+    });
+}
+
+bd_status bd_westervelt_step_index(bd_westervelt* w, int64_t* step) {
+    return guard([&] {
+        if (!w || !step) fail(BD_ERR_INVALID_ARG, "null argument");
+        *step = w->S.step;
+    });
+}
+
+bd_status bd_westervelt_last_ms(bd_westervelt* w, double* ms) {
+    return guard([&] {
+        if (!w || !ms) fail(BD_ERR_INVALID_ARG, "null argument");
+        *ms = w->S.last_ms;
+    });
+}
+
+bd_status bd_westervelt_finish(bd_westervelt* w, bd_westervelt_outputs* out) {
+    return guard([&] {
+        if (!w || !out) fail(BD_ERR_INVALID_ARG, "null argument");
+        ctx_check(w->S.ctx);
+        finish(w->S, out);
+        out->elapsed_ms = w->S.last_ms;
+    });
+}
+
+bd_status bd_westervelt_end(bd_westervelt* w) {
+    return guard([&] {
+        if (!w) return;
+        cudaSetDevice(w->S.ctx->device);
+        cudaStreamSynchronize(w->S.ctx->stream);
+        delete w;
+    });
+}
+
+bd_status bd_checkpoint_size(bd_westervelt* w, size_t* bytes) {
+    return guard([&] {
+        if (!w || !bytes) fail(BD_ERR_INVALID_ARG, "null argument");
+        *bytes = ck_size(w->S);
+    });
+}
+
+bd_status bd_checkpoint_save(bd_westervelt* w, void* blob, size_t bytes) {
+    return guard([&] {
+        if (!w || !blob) fail(BD_ERR_INVALID_ARG, "null argument");
+        ctx_check(w->S.ctx);
+        ck_save(w->S, blob, bytes);
+    });
+}
+
+bd_status bd_checkpoint_load(bd_westervelt* w, const void* blob, size_t bytes) {
+    return guard([&] {
+        if (!w || !blob) fail(BD_ERR_INVALID_ARG, "null argument");
+        ctx_check(w->S.ctx);
+        ck_load(w->S, blob, bytes);
+    });
+}
+
+bd_status bd_westervelt_run(bd_context* ctx, const bd_grid* grid, const bd_medium* medium, const bd_source* source,
+                            const bd_westervelt_params* params, bd_westervelt_outputs* out) {
+    return guard([&] {
+        if (!out) fail(BD_ERR_INVALID_ARG, "null outputs");
+        ctx_check(ctx);
+        bd_westervelt w;
+        setup(w.S, ctx, grid, medium, source, params);
+        timed_advance(w.S, params->n_steps);
+        finish(w.S, out);
+        out->elapsed_ms = w.S.last_ms;
+    });
+}
+
+}  // extern "C"

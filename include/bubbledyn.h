@@ -1,0 +1,402 @@
+/*
+ * bubbledyn.h — C ABI of the GB300 focused-ultrasound engine.
+ *
+ * The reference (FilkinaGramota/BubbleDynamics) has no library interface: it is
+ * three stand-alone programs whose contract is their hard-coded parameter blocks
+ * and their output files.  Each entry point below replaces one of those programs
+ * (or one stage of it) and cites the reference lines it stands in for:
+ *
+ *   W = Westervelt_relax_fft_Pressure_Energy.cu   (pressure / acoustic power)
+ *   T = Westervelt_Temperature_SquareSpiral.cu    (bioheat + CEM43 along a spiral)
+ *   G = Gilmore_liver_3fr_combo.cu                (Gilmore-Zener bubble dynamics)
+ *
+ * Conventions
+ *   - Every call returns a bd_status; no exception crosses the ABI.  The text of
+ *     the last error on the calling thread is returned by bd_last_error_string().
+ *   - The caller owns every host buffer.  A bd_context owns the device memory it
+ *     allocates; one context per host thread.
+ *   - Arrays of cells are x-fastest: idx = (iz*ny + iy)*nx + ix, as in W:155.
+ *   - Calls are blocking unless their name ends in _device (those take device
+ *     pointers and a cudaStream_t passed as void*, and return once enqueued).
+ */
+#ifndef BUBBLEDYN_H
+#define BUBBLEDYN_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BD_ABI_VERSION 1
+
+#define BD_MAX_MATERIALS 8
+#define BD_MAX_RELAX 4
+#define BD_MAX_TONES 4
+#define BD_MAX_DFT 16
+#define BD_MAX_BUBBLE_TONES 9
+
+typedef enum bd_status {
+    BD_OK = 0,
+    BD_ERR_INVALID_ARG = 1,
+    BD_ERR_OOM = 2,
+    BD_ERR_CUDA = 3,
+    BD_ERR_UNSTABLE = 4,        /* NaN/Inf or amplitude blow-up detected in a field */
+    BD_ERR_TIMEOUT = 5,         /* a bounded device wait ran out */
+    BD_ERR_IO = 6,
+    BD_ERR_FAULT_INJECTED = 7,  /* host-side fault injection fired (bd_westervelt_params.fault_at_step) */
+    BD_ERR_UNSUPPORTED = 8,
+    BD_ERR_STATE = 9            /* call out of order (e.g. checkpoint of another geometry) */
+} bd_status;
+
+typedef enum bd_precision { BD_F32 = 0, BD_F64 = 1 } bd_precision;
+
+/* Boundary treatment of one face of the box. */
+typedef enum bd_face_kind {
+    BD_FACE_OPEN = 0,    /* stencil sees p = 0 outside; combine with a sponge */
+    BD_FACE_MUR = 1,     /* first-order Mur ABC on mur_layers layers (W:88-135) */
+    BD_FACE_MIRROR = 2   /* even symmetry plane at index 0: p[-k] = p[k] (W:176-200); x-/y- only */
+} bd_face_kind;
+
+/* ------------------------------------------------------------------------- */
+/* Context and errors                                                         */
+/* ------------------------------------------------------------------------- */
+typedef struct bd_context bd_context;
+
+/* Replaces cudaSetDevice(0) at W:353, T:112, G:436. */
+bd_status bd_context_create(int device, bd_context** out);
+bd_status bd_context_destroy(bd_context* ctx);
+/* Thread-local text of the last error (never NULL). */
+const char* bd_last_error_string(void);
+int bd_abi_version(void);
+/* Number of this library's own kernels launched by the context so far. */
+bd_status bd_context_kernel_launches(bd_context* ctx, int64_t* out);
+
+/* ------------------------------------------------------------------------- */
+/* Westervelt pressure / energy solver (W)                                    */
+/* ------------------------------------------------------------------------- */
+
+/* Mesh.  Mirrors W:406-417 (xy_min, dxy, z_min, dz, dt). */
+typedef struct bd_grid {
+    int32_t nx, ny, nz;         /* cells; the reference uses nx = ny = Nxy (W:410) */
+    int32_t pad0;
+    double x0, y0, z0;          /* coordinate of cell (0,0,0) [m] (W:48-50) */
+    double dx, dz;              /* dy == dx [m] */
+    double dt;                  /* time step [s] (W:416) */
+    int32_t face[6];            /* bd_face_kind of x-, x+, y-, y+, z-, z+ */
+    int32_t mur_layers;         /* Mur layers on MUR faces; 3 in W:108-133 (z- uses source_iz layers) */
+    int32_t sponge_cells;       /* damping layer width on OPEN faces (0 = none) */
+    double sponge_strength;     /* w(d) = exp(-strength*(d/W)^2) applied each step */
+} bd_grid;
+
+/* One acoustic material.  Mirrors the water/tissue blocks W:16-33, W:365-393. */
+typedef struct bd_material {
+    double c0;                  /* sound speed [m/s] (used where no c map is given) */
+    double rho;                 /* density [kg/m^3] */
+    double beta;                /* nonlinearity coefficient */
+    double delta;               /* acoustic diffusivity [m^2/s] */
+    int32_t n_relax;            /* relaxation processes (W hard-codes 2 in tissue, 0 in water) */
+    int32_t pad0;
+    double relax_c[BD_MAX_RELAX];   /* small sound speeds c_nu [m/s] (W:390-391) */
+    double relax_tau[BD_MAX_RELAX]; /* relaxation times tau_nu [s] (W:392-393) */
+    double absorption;          /* alpha [Np/m] at the fundamental, for the water power (W:261) */
+    double harm_absorption;     /* alpha_n = harm_absorption * n*f/1e6 [Np/m] (W:342) */
+} bd_material;
+
+typedef struct bd_medium {
+    int32_t n_materials;
+    int32_t pad0;
+    bd_material mat[BD_MAX_MATERIALS];
+    const int32_t* plane_material;  /* nz entries or NULL: material of each z plane (W:212) */
+    const uint8_t* material_map;    /* nx*ny*nz or NULL: per-cell material (overrides planes) */
+    const float* c_map;             /* nx*ny*nz or NULL: per-cell sound speed (overrides c0) */
+} bd_medium;
+
+typedef enum bd_source_kind {
+    BD_SRC_NONE = 0,
+    BD_SRC_BOWL = 1,            /* spherical bowl projected onto a plane (W:62-85) */
+    BD_SRC_ARRAY = 2            /* same projection, cells grouped into phased-array elements */
+} bd_source_kind;
+
+/* Dirichlet source plane.  Mirrors W:36-42 and W:355-400. */
+typedef struct bd_source {
+    int32_t kind;               /* bd_source_kind */
+    int32_t plane_iz;           /* z index of the source plane; W:75 uses 2 */
+    double focal_length;        /* d [m] (W:38) */
+    double alpha;               /* outer aperture half-angle [rad] (W:39) */
+    double alpha_hole;          /* central hole half-angle [rad] (W:40) */
+    double p0;                  /* on-source pressure amplitude [Pa] (W:42) */
+    double c_delay;             /* sound speed of the geometric delay (W:81 uses c_inf) */
+    double cx, cy;              /* bowl axis position in the plane [m] (0,0 in W) */
+    int32_t n_tones;            /* drive = sum_k amp_k sin(2 pi f_k t' + phase_k) */
+    int32_t pad0;
+    double freq[BD_MAX_TONES];
+    double amp[BD_MAX_TONES];
+    double phase[BD_MAX_TONES];
+    double burst_cycles;        /* 0 = continuous wave (W); else rectangular burst of this many cycles of freq[0] */
+    int32_t n_elements;         /* BD_SRC_ARRAY: number of elements */
+    int32_t pad1;
+    const int32_t* element_of_cell; /* nx*ny: element index of each plane cell or -1 */
+    const double* element_phase;    /* n_elements [rad] */
+    const double* element_amp;      /* n_elements (relative) */
+} bd_source;
+
+typedef enum bd_energy_mode {
+    BD_ENERGY_P2 = 0,           /* E += p^2 dt            (time-integrated intensity * rho c) */
+    BD_ENERGY_DPDT2 = 1         /* E += ((p^{n+1}-p^{n-1})/2dt)^2 dt  (W:253-257) */
+} bd_energy_mode;
+
+/* Time discretisation of the relaxation memory variables. */
+typedef enum bd_relax_scheme {
+    BD_RELAX_REFERENCE = 0,     /* W:226-228: BDF2 memory driven by the backward 5-level d3p/dt3 (W:207);
+                                   amplifies grid-scale modes when (c dt/dx)^2 * 18.1 exceeds ~0.5 */
+    BD_RELAX_SEMI_IMPLICIT = 1  /* same BDF2 memory driven by the 2nd-order d3p/dt3 at t_n through
+                                   p^{n+1}..p^{n-3}, solved per cell; damps every mode up to CFL ~0.39 */
+} bd_relax_scheme;
+
+typedef enum bd_q_mode {
+    BD_Q_NONE = 0,
+    BD_Q_REFERENCE = 1          /* W:261 in water planes, W:341-342 harmonics at iz >= q_iz_split */
+} bd_q_mode;
+
+typedef struct bd_westervelt_params {
+    int32_t precision;          /* bd_precision of the stored fields */
+    int32_t energy_mode;        /* bd_energy_mode */
+    int64_t n_steps;            /* time steps to run */
+    double t0;                  /* time before step 0 [s]; step s runs at t = t0 + (s+1) dt */
+    const double* t_src;        /* optional n_steps source times (W:564 accumulates t += dt) */
+    int64_t peak_start, peak_end;       /* step window [start, end) of the peak |p| map */
+    int64_t energy_start, energy_end;   /* step window of the energy accumulator (W:627) */
+    int64_t dft_start, dft_len;         /* DFT window: samples s = dft_start .. dft_start+dft_len-1 */
+    int32_t n_dft;                      /* frequencies accumulated on the fly (W:663-755 replacement) */
+    int32_t dft_z_lo, dft_z_hi;         /* planes [lo, hi) where the DFT is kept (W:673: tissue) */
+    int32_t q_mode;                     /* bd_q_mode */
+    double dft_freq[BD_MAX_DFT];        /* [Hz]; sample phase = 2 pi f (s - dft_start) dt */
+    int32_t q_iz_split;                 /* W:673 iz_tissue */
+    int32_t q_n_harm;                   /* W:670 N_harm */
+    double q_freq;                      /* fundamental of the Q formulas (W:261, W:342) */
+    int32_t check_every;                /* NaN / blow-up probe interval in steps (0 = off) */
+    int32_t fault_at_step;              /* host-side fault injection: fail at this step (-1 = off) */
+    double blowup_limit;                /* |p| above this counts as unstable (0 = only NaN/Inf) */
+    int32_t graph_chunk;                /* steps per captured CUDA graph (0 = 50, < 0 = plain launches) */
+    int32_t tile_variant;               /* kernel variant (-1 = autotuned / default) */
+    int32_t relax_scheme;               /* bd_relax_scheme */
+    int32_t pad0;
+} bd_westervelt_params;
+
+/* Host output buffers; any may be NULL.  Element type is float for BD_F32 and
+ * double for BD_F64 (Q is always double, as written by W:778-790). */
+typedef struct bd_westervelt_outputs {
+    void* p_final;              /* nx*ny*nz pressure after the last step */
+    void* peak;                 /* nx*ny*nz max |p| over the peak window */
+    void* energy;               /* nx*ny*nz energy accumulator */
+    void* dft_re;               /* n_dft * nx*ny*(dft_z_hi-dft_z_lo) */
+    void* dft_im;
+    double* Q;                  /* nx*ny*nz acoustic power density [W/m^3] (BD_Q_REFERENCE) */
+    double elapsed_ms;          /* device time of the solve (filled by the library) */
+    int64_t steps_done;
+} bd_westervelt_outputs;
+
+/* Full Westervelt solve.  Replaces W:350-790 (the three time loops, the FFT
+ * pass and the result copy) with one fused kernel per step. */
+bd_status bd_westervelt_run(bd_context* ctx, const bd_grid* grid, const bd_medium* medium,
+                            const bd_source* source, const bd_westervelt_params* params,
+                            bd_westervelt_outputs* out);
+
+/* Session form of the same solve: begin, advance in pieces, checkpoint/resume,
+ * finish.  The reference's only checkpoint is the host snapshot at W:600-613
+ * restored at W:690-703. */
+typedef struct bd_westervelt bd_westervelt;
+bd_status bd_westervelt_begin(bd_context* ctx, const bd_grid* grid, const bd_medium* medium,
+                              const bd_source* source, const bd_westervelt_params* params,
+                              bd_westervelt** out);
+bd_status bd_westervelt_advance(bd_westervelt* wv, int64_t n_steps);
+bd_status bd_westervelt_step_index(bd_westervelt* wv, int64_t* step);
+bd_status bd_westervelt_finish(bd_westervelt* wv, bd_westervelt_outputs* out);
+bd_status bd_westervelt_end(bd_westervelt* wv);
+/* Checkpoint blob: header + time-level ring + relaxation state + accumulators. */
+bd_status bd_checkpoint_size(bd_westervelt* wv, size_t* bytes);
+bd_status bd_checkpoint_save(bd_westervelt* wv, void* blob, size_t bytes);
+bd_status bd_checkpoint_load(bd_westervelt* wv, const void* blob, size_t bytes);
+/* Device time of the last advance() in milliseconds. */
+bd_status bd_westervelt_last_ms(bd_westervelt* wv, double* ms);
+
+/* ------------------------------------------------------------------------- */
+/* Adjoint Westervelt (phased-array gradients)                                */
+/* ------------------------------------------------------------------------- */
+
+/* loss = -sum_{focal region} E + side_weight * sum_{side-lobe region} E,
+ * E(x) = sum over the window of p(x)^2 dt.  The focal region is the ball of
+ * radius focal_radius cells around the focus; the side-lobe region is the
+ * focal plane outside side_radius cells. */
+typedef struct bd_focal_loss {
+    int32_t focus_ix, focus_iy, focus_iz;
+    int32_t focal_radius;
+    int32_t side_radius;
+    int32_t pad0;
+    double side_weight;
+    int64_t window_start, window_end;   /* step window [start, end) */
+} bd_focal_loss;
+
+/* Gradient of the loss with respect to element phases and amplitudes of a
+ * BD_SRC_ARRAY source (no counterpart in the reference; the forward model is
+ * W:139-236 + W:62-85).  Uses sqrt(N) checkpointing; FP32 fields. */
+bd_status bd_westervelt_adjoint(bd_context* ctx, const bd_grid* grid, const bd_medium* medium,
+                                const bd_source* source, const bd_westervelt_params* params,
+                                const bd_focal_loss* loss, double* loss_out,
+                                double* grad_phase, double* grad_amp, double* timings_ms);
+
+/* ------------------------------------------------------------------------- */
+/* Bioheat + CEM43 dose along a scan trajectory (T)                           */
+/* ------------------------------------------------------------------------- */
+
+typedef struct bd_thermal_material {
+    double rho;                 /* density [kg/m^3] (T:125, T:132) */
+    double c_t;                 /* specific heat [J/(kg K)] (T:127, T:134) */
+    double k_t;                 /* thermal conductivity [W/(m K)] (T:128, T:135) */
+    double perfusion;           /* Pennes perfusion rate w [1/s] (0 in T) */
+    double T_art;               /* arterial temperature [K] */
+    double T_init;              /* initial temperature [K] (T:149-150) */
+} bd_thermal_material;
+
+typedef struct bd_thermal {
+    int32_t nx, ny, nz;
+    int32_t precision;          /* BD_F64: T in double (T exact); BD_F32: dT from T_ref in float */
+    double dx, dz, dt;          /* T:157-166 */
+    double T_ref;               /* BD_F32 baseline temperature [K] */
+    int32_t n_materials;
+    int32_t dose_init;          /* 1: TD starts at R^(43-T0) dt like T:246-252; 0: zero */
+    bd_thermal_material mat[BD_MAX_MATERIALS];
+    const int32_t* plane_material;  /* nz entries (T:84 split by z) */
+    const uint8_t* material_map;    /* optional nx*ny*nz */
+} bd_thermal;
+
+typedef enum bd_trajectory_kind {
+    BD_TRAJ_SQUARE_SPIRAL = 0,  /* continuous motion of T:141-173, T:323-410 */
+    BD_TRAJ_SPOTS = 1           /* discrete focal spots, each held for a number of steps */
+} bd_trajectory_kind;
+
+typedef struct bd_trajectory {
+    int32_t kind;
+    int32_t n_legs;             /* T:328 spiral_lines */
+    double speed;               /* [m/s] T:141 */
+    double scale;               /* spacing between lines [m] T:142 */
+    double speed_init;          /* T:144 */
+    double t_acc;               /* T:145 */
+    double dxy;                 /* grid step of the shift [m] */
+    double dt;                  /* heat time step [s] */
+    int32_t n_spots;            /* BD_TRAJ_SPOTS */
+    int32_t pad0;
+    const int32_t* spot_sx;     /* shift of Q in cells per spot */
+    const int32_t* spot_sy;
+    const int64_t* spot_steps;  /* heat steps per spot */
+} bd_trajectory;
+
+/* Expand a trajectory into per-step integer shifts of the heat source.
+ * Replaces the host loop T:345-410.  Writes at most cap entries; *n_steps gets
+ * the full count and leg_end[k] (may be NULL, n_legs entries) the step count
+ * after leg/spot k. */
+bd_status bd_trajectory_shifts(const bd_trajectory* traj, int32_t* sx, int32_t* sy,
+                               int64_t cap, int64_t* n_steps, int64_t* leg_end, int32_t leg_cap);
+
+/* Mirror a quarter-domain field (ix,iy >= 0 of W's output .bin, W:778-790)
+ * into the full domain: full[iz][iy][ix] = small[iz][|iy-h|][|ix-h|], h = n_half
+ * (T:269-306).  small has (n_half+1)^2 cells per plane. */
+bd_status bd_unfold_quarter(const double* small, int32_t n_half, int32_t nz, double* full);
+
+typedef struct bd_heat_outputs {
+    double* T_final;            /* nx*ny*nz temperature [K] */
+    double* dose;               /* nx*ny*nz CEM43 dose [s] */
+    double* snapshots;          /* n_snap * nx*ny*nz temperature [K] after the listed legs (T:411-563) */
+    const int32_t* snapshot_legs;  /* leg numbers (1-based) after which to copy T */
+    int32_t n_snap;
+    int32_t pad0;
+    double elapsed_ms;
+    int64_t steps_done;
+} bd_heat_outputs;
+
+/* Heat + dose run over a trajectory with a fixed source Q (full domain, W/m^3)
+ * shifted by the trajectory.  Replaces T:345-573. */
+bd_status bd_spiral_heat_run(bd_context* ctx, const bd_thermal* thermal, const double* Q,
+                             const bd_trajectory* traj, int64_t max_steps,
+                             bd_heat_outputs* out);
+
+/* ------------------------------------------------------------------------- */
+/* Gilmore-Zener bubble dynamics (G)                                          */
+/* ------------------------------------------------------------------------- */
+
+/* Medium constants, G:13-23 / G:440-450. */
+typedef struct bd_gilmore_medium {
+    double rho, P0, S2, mu4, G4_3, C_inf, lambda, n, B, gamma;
+} bd_gilmore_medium;
+
+/* Drive: P(t) = sum_k a[k] sin(2 pi f[k] t + phi[k]).  bd_gilmore_combo_tones()
+ * builds the single/dual/triple normalisation of G:40-57. */
+typedef struct bd_bubble {
+    double R0;
+    int32_t n_tones;
+    int32_t pad0;
+    double f[BD_MAX_BUBBLE_TONES];
+    double a[BD_MAX_BUBBLE_TONES];
+    double phi[BD_MAX_BUBBLE_TONES];
+} bd_bubble;
+
+typedef struct bd_ode_params {
+    double t_end;               /* integration end [s] */
+    double h0;                  /* first step (G:355: 1e-13) */
+    double atol, rtol;          /* G:214-215 use 1e-9 / 1e-9 */
+    double fac_max;             /* G:244: 5 */
+    int64_t max_steps;          /* per-bubble attempt cap (flagged, never a hang) */
+    int32_t stop_at_threshold;  /* 1: stop when R' <= -C_inf (G:313) */
+    int32_t ref_arith;          /* 1: evaluate the RHS in the reference's operation order (no FSAL) */
+} bd_ode_params;
+
+typedef enum bd_bubble_status {
+    BD_BUBBLE_DONE = 0,
+    BD_BUBBLE_THRESHOLD = 1,    /* stopped at R' <= -C_inf */
+    BD_BUBBLE_STEP_CAP = 2,
+    BD_BUBBLE_NONFINITE = 3
+} bd_bubble_status;
+
+typedef struct bd_bubble_result {
+    double R, Rdot, tau, q, t;
+    double R_max, R_min;
+    double t_threshold;         /* first time R' <= -C_inf, or -1 */
+    int64_t n_accept, n_reject;
+    int32_t status;             /* bd_bubble_status */
+    int32_t threshold;          /* 1 if R' <= -C_inf was reached */
+} bd_bubble_result;
+
+/* The single/dual/triple drive of G:40-57 for amplitude A and frequencies
+ * f1 <= f2 <= f3 as tones (phases phi may be NULL = 0). */
+bd_status bd_gilmore_combo_tones(double A, const double f[3], const double* phi, bd_bubble* b);
+
+/* Frequency combinations of G:498-520: log-spaced n_fr frequencies in
+ * [f_min, f_max], ordered triples i <= ii <= iii excluding i < ii == iii.
+ * Writes 3*n entries into out (cap triples); *n_combo gets the count. */
+bd_status bd_gilmore_combos(int32_t n_fr, double f_min, double f_max, double* out,
+                            int64_t cap, int64_t* n_combo);
+
+/* Forward integration of n bubbles with a persistent work-stealing kernel.
+ * The integrator is G:183-318 (Dormand-Prince 5(4)); G itself only runs it
+ * inside the threshold search. */
+bd_status bd_gilmore_run(bd_context* ctx, const bd_gilmore_medium* medium, int64_t n,
+                         const bd_bubble* bubbles, const bd_ode_params* ode,
+                         bd_bubble_result* results, double* elapsed_ms);
+bd_status bd_gilmore_run_device(bd_context* ctx, const bd_gilmore_medium* medium, int64_t n,
+                                const bd_bubble* d_bubbles, const bd_ode_params* ode,
+                                bd_bubble_result* d_results, void* stream);
+
+/* Threshold search of G:323-429 for every (combo, R0) pair; results are
+ * combo-major (results[i_combo*n_R0 + i_R0]) like G:598.  A = 1e7 means no
+ * cavitation up to 10 MPa; -1 is never left behind (G:359 initial value). */
+bd_status bd_gilmore_threshold(bd_context* ctx, const bd_gilmore_medium* medium,
+                               const double* fr_combo, int64_t n_combo,
+                               const double* R0, int64_t n_R0, int32_t ref_arith,
+                               int64_t max_steps, double* results, double* elapsed_ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BUBBLEDYN_H */

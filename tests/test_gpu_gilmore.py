@@ -1,0 +1,107 @@
+"""Gilmore-Zener integrator on the GPU against the CPU checker and fixtures
+of the reference's own DPRK_step and threshold kernel."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from bubbledynamics_gb300 import abi, api, presets
+from tests.conftest import golden_path
+
+pytestmark = pytest.mark.gpu
+
+
+def to_ctypes(b):
+    return (abi.Bubble * len(b)).from_buffer_copy(b.tobytes())
+
+
+def combo_bubbles(lib, R0, A, f3):
+    b = np.zeros(len(R0), api.BUBBLE_DTYPE)
+    for i in range(len(R0)):
+        bb = abi.Bubble()
+        bb.R0 = R0[i]
+        api.check(lib.bd_gilmore_combo_tones(float(A[i]), np.ascontiguousarray(f3[i]).ctypes.data, None, C.byref(bb)))
+        b[i] = np.frombuffer(bytes(bb), dtype=api.BUBBLE_DTYPE)[0]
+    return b
+
+
+def test_fast_path_matches_oracle(ctx, oracle):
+    med = presets.cfg2_medium()
+    b = presets.cfg2_bubbles(64, seed=5)
+    b["a"] *= 0.15                      # moderate drive: smooth, non-collapsing trajectories
+    ode = presets.cfg2_ode(t_end=10e-6, atol=1e-14, rtol=1e-8)
+    res, ms = ctx.gilmore(med, b, ode)
+    ro = oracle.gilmore(med, to_ctypes(b), ode)
+    R = np.array([r.R for r in ro])
+    Rmax = np.array([r.R_max for r in ro])
+    assert np.all(res["status"] == abi.BD_BUBBLE_DONE)
+    np.testing.assert_allclose(res["t"], 10e-6, rtol=1e-12)
+    np.testing.assert_allclose(res["R"], R, rtol=1e-6)
+    np.testing.assert_allclose(res["R_max"], Rmax, rtol=1e-6)
+
+
+def test_ref_arith_matches_reference_fixture(ctx, lib):
+    """G's own DPRK_step loop (fixture) vs the GPU's reference-arithmetic path:
+    moderate drives to endT, and a strong drive stopped at the threshold."""
+    g = np.load(golden_path("G_forward.npz"))
+    b = combo_bubbles(lib, g["R0"], g["A"], g["f3"])
+    for stop, sl in ((0, slice(0, 4)), (1, slice(4, 5))):
+        ode = abi.OdeParams()
+        ode.t_end, ode.h0, ode.atol, ode.rtol, ode.fac_max = float(g["endT"]), 1e-13, 1e-9, 1e-9, 5.0
+        ode.max_steps, ode.stop_at_threshold, ode.ref_arith = 200000, stop, 1
+        res, _ = ctx.gilmore(presets.ref_G_medium(), b[sl], ode)
+        np.testing.assert_allclose(res["n_accept"], g["counts"][sl], rtol=1e-3)
+        np.testing.assert_allclose(res["t"], g["state"][sl][:, 0], rtol=1e-9)
+        np.testing.assert_allclose(res["R"], g["state"][sl][:, 1], rtol=1e-6)
+        if stop:
+            assert np.all(res["status"] == abi.BD_BUBBLE_THRESHOLD)
+            np.testing.assert_allclose(res["t_threshold"], g["thr"][sl], rtol=1e-6)
+
+
+def test_threshold_matches_reference_fixture(ctx):
+    g = np.load(golden_path("G_threshold.npz"))
+    A, ms = ctx.gilmore_threshold(presets.ref_G_medium(), g["combos"], g["R0"], ref_arith=1)
+    d = np.abs(A - g["A"])
+    print("threshold: %d/%d exact, max diff %.0f Pa" % ((d == 0).sum(), d.size, d.max()))
+    assert np.all(d <= 1000.0)
+    assert (d == 0).mean() >= 0.9
+
+
+def test_threshold_fast_path_close(ctx):
+    g = np.load(golden_path("G_threshold.npz"))
+    A, ms = ctx.gilmore_threshold(presets.ref_G_medium(), g["combos"], g["R0"], ref_arith=0)
+    assert np.all(np.abs(A - g["A"]) <= 2000.0)
+
+
+def test_every_bubble_processed_once(ctx):
+    med = presets.cfg2_medium()
+    n = 3000
+    b = presets.cfg2_bubbles(n, seed=7)
+    b["a"] *= 0.2
+    ode = presets.cfg2_ode(t_end=1e-6, atol=1e-12, rtol=1e-8)
+    res, ms = ctx.gilmore(med, b, ode)
+    assert np.all(res["status"] == abi.BD_BUBBLE_DONE)
+    np.testing.assert_allclose(res["t"], 1e-6, rtol=1e-12)
+    assert np.all(res["n_accept"] > 0)
+    # each bubble's own R0: the result row belongs to its bubble
+    assert np.all(np.abs(res["R"] / b["R0"] - 1.0) < 0.5)
+
+
+def test_step_cap_flagged(ctx):
+    med = presets.cfg2_medium()
+    b = presets.cfg2_bubbles(40, seed=8)
+    ode = presets.cfg2_ode(t_end=50e-6, max_steps=100)
+    res, ms = ctx.gilmore(med, b, ode)
+    assert np.all(res["status"] == abi.BD_BUBBLE_STEP_CAP)
+    assert np.all(res["n_accept"] == 100)
+
+
+def test_stop_at_threshold(ctx):
+    med = presets.cfg2_medium()
+    b = presets.cfg2_bubbles(64, seed=9)
+    ode = presets.cfg2_ode(t_end=20e-6)
+    ode.stop_at_threshold = 1
+    res, ms = ctx.gilmore(med, b, ode)
+    hit = res["status"] == abi.BD_BUBBLE_THRESHOLD
+    assert np.all(res["threshold"][hit] == 1)
+    assert np.all(res["Rdot"][hit] <= -med.C_inf)

@@ -1,0 +1,78 @@
+"""Bioheat + CEM43 dose on the GPU against the reference's own kernel
+(fixture) and the CPU checker."""
+import numpy as np
+import pytest
+
+from bubbledynamics_gb300 import abi, api, presets
+from tests.conftest import golden_path
+
+pytestmark = pytest.mark.gpu
+
+
+def mini():
+    from tests.golden.make_golden import t_mini_inputs
+    return t_mini_inputs()
+
+
+def test_heat_f64_matches_reference_fixture(ctx):
+    g = np.load(golden_path("T_mini.npz"))
+    k, prob, sx, sy, Q = mini()
+    r = ctx.heat(prob.thermal, Q, prob.traj)
+    assert r["steps_done"] == int(g["n_steps"])
+    np.testing.assert_allclose(r["T"], g["T"], rtol=1e-13, atol=0)
+    np.testing.assert_allclose(r["dose"], g["TD"], rtol=1e-11, atol=0)
+
+
+def test_heat_f32_close_to_oracle(ctx, oracle):
+    k, prob, sx, sy, Q = mini()
+    T0, TD0 = prob.initial_fields()
+    To, TDo, _ = oracle.heat(prob.thermal, Q, sx, sy, T0, TD0)
+    p32 = presets.make_ref_T(k, precision=abi.BD_F32)
+    r = ctx.heat(p32.thermal, Q, p32.traj)
+    rise = To.reshape(prob.shape) - T0
+    err_T = np.abs(r["T"] - To.reshape(prob.shape)).max() / np.abs(rise).max()
+    err_D = np.abs(r["dose"] - TDo.reshape(prob.shape)).max() / np.abs(TDo).max()
+    print("heat f32: max |dT| error / max rise %.3g, dose %.3g" % (err_T, err_D))
+    assert err_T < 1e-5
+    assert err_D < 1e-5
+
+
+def test_heat_snapshots_and_spots(ctx, oracle):
+    k, prob, sx, sy, Q = mini()
+    prob.set_spots([0, 4, -3], [0, 2, 5], [40, 30, 25])
+    ssx, ssy, legs = api.trajectory_shifts(prob.traj)
+    T0, TD0 = prob.initial_fields()
+    To, TDo, snaps = oracle.heat(prob.thermal, Q, ssx, ssy, T0, TD0, snap_steps=[40, 70])
+    r = ctx.heat(prob.thermal, Q, prob.traj, snapshot_legs=[1, 2])
+    np.testing.assert_allclose(r["snapshots"][0].reshape(-1), snaps[0], rtol=1e-13)
+    np.testing.assert_allclose(r["snapshots"][1].reshape(-1), snaps[1], rtol=1e-13)
+    np.testing.assert_allclose(r["T"].reshape(-1), To, rtol=1e-13)
+
+
+def test_pennes_perfusion_decay(ctx):
+    """No source, uniform excess temperature: T - T_art decays as (1 - w dt)^n."""
+    k, prob, sx, sy, Q = mini()
+    for m in range(prob.thermal.n_materials):
+        prob.thermal.mat[m].perfusion = 0.5
+        prob.thermal.mat[m].T_art = 310.0
+        prob.thermal.mat[m].T_init = 315.0
+        prob.thermal.mat[m].k_t = 0.0
+    prob.set_spots([0], [0], [200])
+    r = ctx.heat(prob.thermal, np.zeros(prob.shape), prob.traj, want_dose=False)
+    expect = 310.0 + 5.0 * (1.0 - 0.5 * prob.thermal.dt) ** 200
+    inner = r["T"][1:-1, 1:-1, 1:-1]
+    np.testing.assert_allclose(inner, expect, rtol=1e-12)
+
+
+def test_cem43_constant_temperatures(ctx):
+    """Constant 44 C for 1 s adds 2 s of dose per second, 42 C adds 0.25 s/s."""
+    k, prob, sx, sy, Q = mini()
+    for T_c, rate in ((44.0, 2.0), (42.0, 0.25)):
+        for m in range(prob.thermal.n_materials):
+            prob.thermal.mat[m].T_init = 273.15 + T_c
+            prob.thermal.mat[m].k_t = 0.0
+        prob.thermal.dose_init = 0
+        prob.set_spots([0], [0], [1000])
+        r = ctx.heat(prob.thermal, np.zeros(prob.shape), prob.traj)
+        inner = r["dose"][1:-1, 1:-1, 1:-1]
+        np.testing.assert_allclose(inner, rate * 1.0, rtol=1e-9)

@@ -1,0 +1,194 @@
+"""Westervelt solver on the GPU (through the C ABI) against the CPU checker and
+against fixtures of the reference's own code.
+
+Tolerances: FP64 fields agree with the FP64 checker to 1e-9 relative L2 (the
+GPU contracts a*b+c into FMAs and uses its own sin); FP32 fields are held to
+the 1e-5 relative L2 field accuracy of the FP32 design (peak and energy
+maps), measured against the FP64 checker."""
+import numpy as np
+import pytest
+
+from bubbledynamics_gb300 import abi, api, presets
+from tests.conftest import golden_path
+
+pytestmark = pytest.mark.gpu
+
+
+def rel_l2(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+@pytest.fixture(scope="module")
+def ref_mini_oracle(oracle):
+    prob = presets.ref_W_mini(abi.BD_F64)
+    return prob, oracle.westervelt(prob)
+
+
+def test_ref_mini_f64_matches_oracle(ctx, ref_mini_oracle):
+    prob, exp = ref_mini_oracle
+    got = ctx.westervelt(prob)
+    assert got["steps_done"] == prob.params.n_steps
+    assert rel_l2(got["p_final"], exp["p_final"]) < 1e-9
+    assert rel_l2(got["peak"], exp["peak"]) < 1e-9
+    assert rel_l2(got["Q"], exp["Q"]) < 1e-9
+
+
+def test_ref_mini_f64_matches_reference_fixture(ctx):
+    """The full W program on a small box: pressure snapshot after the first
+    loop and the acoustic power Q of the reference's own kernels."""
+    g = np.load(golden_path("W_mini.npz"))
+    prob = presets.ref_W_mini(abi.BD_F64)
+    p1 = prob.copy()
+    p1.params.n_steps = prob.meta["n_loop1"]
+    P = ctx.westervelt(p1, want=("p_final",))["p_final"]
+    assert rel_l2(P[g["planes"]], g["P"]) < 1e-9
+    Q = ctx.westervelt(prob, want=("Q",))["Q"]
+    assert rel_l2(Q[g["planes"]], g["Q"]) < 2e-6      # the reference transforms in FP32 (cuFFT C2C)
+
+
+def test_ref_mini_f32_close_to_oracle(ctx, ref_mini_oracle):
+    prob, exp = ref_mini_oracle
+    p32 = presets.ref_W_mini(abi.BD_F32)
+    got = ctx.westervelt(p32)
+    e_p = rel_l2(got["p_final"], exp["p_final"])
+    e_q = rel_l2(got["Q"], exp["Q"])
+    print("ref_mini f32: p_final %.3g  Q %.3g" % (e_p, e_q))
+    assert e_p < 1e-4
+    assert e_q < 1e-4
+
+
+@pytest.fixture(scope="module")
+def cfg1_small_oracle(oracle):
+    prob = presets.cfg1(48, 48, 96, 600, precision=abi.BD_F64)
+    return prob, oracle.westervelt(prob)
+
+
+def test_cfg1_small_f32_field_accuracy(ctx, cfg1_small_oracle):
+    """FP32 kernel vs FP64 checker on the benchmark physics (heterogeneous c,
+    relaxation, sponge, burst): output maps within 1e-5 relative L2."""
+    prob64, exp = cfg1_small_oracle
+    prob = presets.cfg1(48, 48, 96, 600, precision=abi.BD_F32)
+    got = ctx.westervelt(prob)
+    e = {k: rel_l2(got[k], exp[k]) for k in ("peak", "energy", "p_final")}
+    print("cfg1 small f32 errors:", e)
+    assert e["peak"] < 1e-5
+    assert e["energy"] < 1e-5
+
+
+def test_cfg1_small_f64_matches_oracle(ctx, cfg1_small_oracle):
+    prob64, exp = cfg1_small_oracle
+    got = ctx.westervelt(prob64)
+    for k in ("p_final", "peak", "energy"):
+        assert rel_l2(got[k], exp[k]) < 1e-9, k
+
+
+def test_graph_and_plain_launches_identical(ctx):
+    a = presets.cfg1(40, 40, 64, 230, precision=abi.BD_F32)
+    b = presets.cfg1(40, 40, 64, 230, precision=abi.BD_F32)
+    a.params.graph_chunk = 20
+    b.params.graph_chunk = -1
+    ra = ctx.westervelt(a)
+    rb = ctx.westervelt(b)
+    for k in ("p_final", "peak", "energy"):
+        np.testing.assert_array_equal(ra[k], rb[k])
+
+
+def test_all_tile_variants_identical(ctx):
+    base = None
+    for v in range(8):
+        p = presets.cfg1(40, 40, 72, 60, precision=abi.BD_F32)
+        p.params.tile_variant = v
+        r = ctx.westervelt(p, want=("p_final", "peak"))
+        if base is None:
+            base = r
+        else:
+            np.testing.assert_array_equal(r["p_final"], base["p_final"])
+            np.testing.assert_array_equal(r["peak"], base["peak"])
+
+
+def test_run_twice_bitwise(ctx):
+    p = presets.ref_W_mini(abi.BD_F32, Nxy=24, Nz=40, loop1_periods=1, periods=1)
+    a = ctx.westervelt(p)
+    b = ctx.westervelt(p)
+    for k in ("p_final", "Q", "dft_re"):
+        np.testing.assert_array_equal(a[k], b[k])
+
+
+def test_checkpoint_resume_bitwise(ctx):
+    p = presets.ref_W_mini(abi.BD_F32, Nxy=24, Nz=40, loop1_periods=1, periods=1)
+    full = ctx.westervelt(p)
+    n = p.params.n_steps
+    with ctx.westervelt_session(p) as s:
+        s.advance(137)
+        assert s.step() == 137
+        blob = s.checkpoint()
+    with ctx.westervelt_session(p) as s2:
+        s2.restore(blob)
+        assert s2.step() == 137
+        s2.advance(n - 137)
+        res = s2.finish()
+    for k in ("p_final", "peak", "energy", "Q", "dft_re", "dft_im"):
+        np.testing.assert_array_equal(res[k], full[k])
+
+
+def test_fault_injection_then_resume(ctx):
+    """A host-side fault at step k stops the solve there; resuming from a
+    checkpoint taken at the fault reproduces the uninterrupted result."""
+    p = presets.ref_W_mini(abi.BD_F32, Nxy=24, Nz=40, loop1_periods=1, periods=1)
+    full = ctx.westervelt(p)
+    pf = p.copy()
+    pf.params.fault_at_step = 75
+    with ctx.westervelt_session(pf) as s:
+        with pytest.raises(api.BDError) as ei:
+            s.advance(pf.params.n_steps)
+        assert ei.value.status == abi.BD_ERR_FAULT_INJECTED
+        assert s.step() == 75
+        blob = s.checkpoint()
+    with ctx.westervelt_session(p) as s2:
+        s2.restore(blob)
+        s2.advance(p.params.n_steps - 75)
+        res = s2.finish()
+    np.testing.assert_array_equal(res["p_final"], full["p_final"])
+    np.testing.assert_array_equal(res["Q"], full["Q"])
+
+
+def test_blowup_probe_reports_unstable(ctx):
+    p = presets.cfg1(32, 32, 48, 100, precision=abi.BD_F32)
+    p.params.check_every = 10
+    p.params.blowup_limit = 1.0          # any pressure above 1 Pa counts as a blow-up
+    with pytest.raises(api.BDError) as ei:
+        ctx.westervelt(p, want=("peak",))
+    assert ei.value.status == abi.BD_ERR_UNSTABLE
+
+
+def test_checkpoint_of_other_geometry_rejected(ctx):
+    a = presets.cfg1(32, 32, 48, 20, precision=abi.BD_F32)
+    b = presets.cfg1(32, 32, 56, 20, precision=abi.BD_F32)
+    with ctx.westervelt_session(a) as s:
+        s.advance(10)
+        blob = s.checkpoint()
+    with ctx.westervelt_session(b) as s2:
+        with pytest.raises(api.BDError) as ei:
+            s2.restore(blob)
+        assert ei.value.status == abi.BD_ERR_STATE
+
+
+def test_invalid_arguments(ctx):
+    p = presets.cfg1(32, 32, 48, 20, precision=abi.BD_F32)
+    p.params.precision = 7
+    with pytest.raises(api.BDError) as ei:
+        ctx.westervelt(p)
+    assert ei.value.status == abi.BD_ERR_INVALID_ARG
+    q = presets.cfg1(32, 32, 48, 20, precision=abi.BD_F32)
+    q.source.plane_iz = 999
+    with pytest.raises(api.BDError):
+        ctx.westervelt(q)
+
+
+def test_kernel_launches_counted(ctx):
+    before = ctx.kernel_launches()
+    p = presets.cfg1(32, 32, 48, 30, precision=abi.BD_F32)
+    ctx.westervelt(p, want=("peak",))
+    assert ctx.kernel_launches() - before >= 30
