@@ -22,14 +22,22 @@
 #include <tuple>
 #include <vector>
 
+#include <cudaTypedefs.h>
+
 #include "bd_internal.h"
 #include "wv_kernels.cuh"
+#include "wv_tma.cuh"
 
 namespace bd {
 
-struct Variant { int tx, ty, zb; };
+// Kernel variants: 0-7 plain (read-only-cache neighbours), 8-15 TMA-pipelined
+// (need a row pitch that is a multiple of 16 bytes).
+struct Variant { int tx, ty, zb, tma; };
 static const Variant kVariants[] = {
-    {32, 8, 32}, {32, 4, 32}, {64, 4, 32}, {32, 8, 64}, {32, 16, 16}, {64, 8, 16}, {128, 2, 32}, {32, 8, 0},
+    {32, 8, 32, 0}, {32, 4, 32, 0}, {64, 4, 32, 0}, {32, 8, 64, 0},
+    {32, 16, 16, 0}, {64, 8, 16, 0}, {128, 2, 32, 0}, {32, 8, 0, 0},
+    {32, 4, 32, 1}, {32, 8, 32, 1}, {64, 4, 32, 1}, {32, 4, 16, 1},
+    {32, 8, 16, 1}, {64, 4, 16, 1}, {32, 4, 64, 1}, {64, 2, 32, 1},
 };
 static const int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
@@ -64,6 +72,9 @@ struct WvSession {
     double last_ms = 0.0;
     cudaGraphExec_t graph = nullptr;
     int graph_variant = -1;
+    // tensor maps of the TMA variant in use (built per tile shape)
+    int maps_tx = 0, maps_ty = 0;
+    CUtensorMap mP0[5], mQ[5], mR[BD_MAX_RELAX][2], mC, mPeak, mEnergy;
     std::vector<bd_material> mats;
     int n_materials = 0;
     bool has_cmap = false, has_matmap = false, has_planemat = false;
@@ -110,7 +121,7 @@ static WvArgs<real> make_args(WvSession& S, int64_t s) {
     a.yhi = a.mur_yp ? S.ny - 1 - a.L : S.ny - 1;
     a.zlo = a.Lzm;
     a.zhi = a.mur_zp ? S.nz - 1 - a.L : S.nz - 1;
-    if (g.sponge_cells > 0) { a.wx = S.wx.as<float>(); a.wy = S.wy.as<float>(); a.wz = S.wz.as<float>(); }
+    if (g.sponge_cells > 0) { a.wx = S.wx.as<real>(); a.wy = S.wy.as<real>(); a.wz = S.wz.as<real>(); }
     a.dt = (real)g.dt;
     a.kxy180 = (real)(g.dt * g.dt / (g.dx * g.dx) / 180.0);
     a.kz180 = (real)(g.dt * g.dt / (g.dz * g.dz) / 180.0);
@@ -147,6 +158,81 @@ static WvArgs<real> make_args(WvSession& S, int64_t s) {
     return a;
 }
 
+static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        BD_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q));
+        if (q != cudaDriverEntryPointSuccess || !p) fail(BD_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
+        fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }
+    return fn;
+}
+
+static CUtensorMap make_map(const WvSession& S, const void* base, bool is_float, int bx, int by) {
+    CUtensorMap m;
+    const size_t esz = is_float ? 4 : 8;
+    cuuint64_t dims[3] = {(cuuint64_t)S.nx, (cuuint64_t)S.ny, (cuuint64_t)S.nz};
+    cuuint64_t strides[2] = {(cuuint64_t)S.nx * esz, (cuuint64_t)S.nx * S.ny * esz};
+    cuuint32_t box[3] = {(cuuint32_t)bx, (cuuint32_t)by, 1};
+    cuuint32_t estr[3] = {1, 1, 1};
+    CUresult r = encode_fn()(&m, is_float ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3,
+                             const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                             CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) fail(BD_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return m;
+}
+
+static bool tma_eligible(const WvSession& S) {
+    return (S.nx * S.esz) % 16 == 0 && S.nx >= 8;
+}
+
+static void build_maps(WvSession& S, int tx, int ty) {
+    if (S.maps_tx == tx && S.maps_ty == ty) return;
+    const bool f = S.prec == BD_F32;
+    for (int k = 0; k < 5; ++k) {
+        S.mP0[k] = make_map(S, S.P[k].p, f, tx + 8, ty + 6);
+        S.mQ[k] = make_map(S, S.P[k].p, f, tx, ty);
+    }
+    for (int v = 0; v < S.max_relax; ++v)
+        for (int k = 0; k < 2; ++k) S.mR[v][k] = make_map(S, S.R[v][k].p, f, tx, ty);
+    S.mPeak = make_map(S, S.peak.p, f, tx, ty);
+    S.mEnergy = make_map(S, S.energy.p, f, tx, ty);
+    if (S.has_cmap) S.mC = make_map(S, S.cmap.p, true, tx, ty);
+    S.maps_tx = tx;
+    S.maps_ty = ty;
+}
+
+template <class real, int TX, int TY>
+static void launch_tma_t(WvSession& S, const WvArgs<real>& a, int64_t s, int koff, cudaStream_t st) {
+    using L = TmaLayout<real, TX, TY>;
+    build_maps(S, TX, TY);
+    TmaMaps maps;
+    std::memset(&maps, 0, sizeof maps);
+    const int h = head_of(s);
+    maps.p0 = S.mP0[h];
+    for (int k = 0; k < 4; ++k) maps.q[k] = S.mQ[(h + 1 + k) % 5];
+    const int rh = (int)(s & 1);
+    for (int v = 0; v < S.max_relax; ++v) { maps.rc[v] = S.mR[v][rh]; maps.ro[v] = S.mR[v][rh ^ 1]; }
+    maps.peak = S.mPeak;
+    maps.energy = S.mEnergy;
+    if (S.has_cmap) maps.cmap = S.mC;
+    const int smem = L::smem(S.max_relax, S.has_cmap);
+    static bool attr_set[2][64][64] = {};
+    bool& done = attr_set[sizeof(real) == 8][TX % 64][TY % 64];
+    if (!done) {
+        BD_CUDA(cudaFuncSetAttribute(wv_tma_kernel<real, TX, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        done = true;
+    }
+    dim3 block(TX, TY, 1);
+    dim3 grid((S.nx + TX - 1) / TX, (S.ny + TY - 1) / TY, (S.nz + a.zb - 1) / a.zb);
+    wv_tma_kernel<real, TX, TY><<<grid, block, smem, st>>>(a, S.kconst.as<WvConst<real>>(), koff, maps,
+                                                            S.flag.as<unsigned>() + 1);
+    BD_LAUNCHED(S.ctx);
+}
+
 template <class real, int TX, int TY>
 static void launch_step_t(WvSession& S, const WvArgs<real>& a, int koff, cudaStream_t st) {
     dim3 block(TX, TY, 1);
@@ -160,6 +246,7 @@ static void launch_step(WvSession& S, int variant, int64_t s, int koff, cudaStre
     WvArgs<real> a = make_args<real>(S, s);
     const Variant& v = kVariants[variant];
     a.zb = v.zb > 0 ? v.zb : S.nz;
+    if (v.tma && !tma_eligible(S)) fail(BD_ERR_INVALID_ARG, "tile variant %d needs a 16-byte row pitch", variant);
     switch (variant) {
         case 0: case 3: case 7: launch_step_t<real, 32, 8>(S, a, koff, st); break;
         case 1: launch_step_t<real, 32, 4>(S, a, koff, st); break;
@@ -167,6 +254,10 @@ static void launch_step(WvSession& S, int variant, int64_t s, int koff, cudaStre
         case 4: launch_step_t<real, 32, 16>(S, a, koff, st); break;
         case 5: launch_step_t<real, 64, 8>(S, a, koff, st); break;
         case 6: launch_step_t<real, 128, 2>(S, a, koff, st); break;
+        case 8: case 11: case 14: launch_tma_t<real, 32, 4>(S, a, s, koff, st); break;
+        case 9: case 12: launch_tma_t<real, 32, 8>(S, a, s, koff, st); break;
+        case 10: case 13: launch_tma_t<real, 64, 4>(S, a, s, koff, st); break;
+        case 15: launch_tma_t<real, 64, 2>(S, a, s, koff, st); break;
         default: fail(BD_ERR_INVALID_ARG, "bad tile variant %d", variant);
     }
     if (S.any_mur) {
@@ -292,6 +383,7 @@ static void zero_state(WvSession& S) {
     BD_CUDA(cudaMemsetAsync(S.energy.p, 0, S.energy.bytes, st));
     if (S.dre.p) { BD_CUDA(cudaMemsetAsync(S.dre.p, 0, S.dre.bytes, st)); BD_CUDA(cudaMemsetAsync(S.dim.p, 0, S.dim.bytes, st)); }
     BD_CUDA(cudaMemsetAsync(S.step_base.p, 0, sizeof(long long), st));
+    BD_CUDA(cudaMemsetAsync(S.flag.p, 0, 64, st));
     S.step = 0;
 }
 
@@ -317,6 +409,7 @@ static void autotune(WvSession& S) {
     const int reps = 4;
     for (int v = 0; v < kNumVariants; ++v) {
         if (kVariants[v].zb == 0 && S.nz > 512) continue;
+        if (kVariants[v].tma && !tma_eligible(S)) continue;
         issue_steps(S, v, S.step, 2, st);  // warm-up
         S.step += 2;
         BD_CUDA(cudaEventRecord(S.ctx->ev0, st));
@@ -458,20 +551,24 @@ static void setup(WvSession& S, bd_context* ctx, const bd_grid* g, const bd_medi
     // sponge profiles w(d) = exp(-strength (d/W)^2) on OPEN faces
     {
         auto prof = [&](int n, int lo, int hi) {
-            std::vector<float> w(n, 1.0f);
+            std::vector<double> w(n, 1.0);
             const int W = g->sponge_cells;
             for (int i = 0; i < n && W > 0; ++i) {
                 double f = 1.0;
                 if (lo == BD_FACE_OPEN && i < W) { double d = (double)(W - i) / W; f *= std::exp(-g->sponge_strength * d * d); }
                 if (hi == BD_FACE_OPEN && i >= n - W) { double d = (double)(i - (n - W) + 1) / W; f *= std::exp(-g->sponge_strength * d * d); }
-                w[i] = (float)f;
+                w[i] = f;
             }
             return w;
         };
+        auto up = [&](PoolBuf& b, const std::vector<double>& w) {
+            if (S.prec == BD_F64) upload(S, b, w);
+            else upload(S, b, std::vector<float>(w.begin(), w.end()));
+        };
         if (g->sponge_cells > 0) {
-            upload(S, S.wx, prof(S.nx, g->face[0], g->face[1]));
-            upload(S, S.wy, prof(S.ny, g->face[2], g->face[3]));
-            upload(S, S.wz, prof(S.nz, g->face[4], g->face[5]));
+            up(S.wx, prof(S.nx, g->face[0], g->face[1]));
+            up(S.wy, prof(S.ny, g->face[2], g->face[3]));
+            up(S.wz, prof(S.nz, g->face[4], g->face[5]));
         }
     }
     // source plane (W:62-85): amplitude, var, delay per plane cell
@@ -711,6 +808,9 @@ static double timed_advance(WvSession& S, int64_t n) {
     float ms = 0;
     BD_CUDA(cudaEventElapsedTime(&ms, S.ctx->ev0, S.ctx->ev1));
     S.last_ms = ms;
+    unsigned f = 0;
+    BD_CUDA(cudaMemcpy(&f, S.flag.as<unsigned>() + 1, sizeof f, cudaMemcpyDeviceToHost));
+    if (f & 4u) fail(BD_ERR_TIMEOUT, "a pipeline wait in the stencil kernel timed out");
     return ms;
 }
 

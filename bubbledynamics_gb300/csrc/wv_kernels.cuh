@@ -57,9 +57,9 @@ struct WvArgs {
     int src_iz;                // source plane or -1
     int mir_x, mir_y;
     int mur_xp, mur_yp, mur_zp, mur_zm, L, Lzm;
-    const float* __restrict__ wx;   // sponge factors per axis (nullptr = none)
-    const float* __restrict__ wy;
-    const float* __restrict__ wz;
+    const real* __restrict__ wx;    // sponge factors per axis (nullptr = none)
+    const real* __restrict__ wy;
+    const real* __restrict__ wz;
     real dt, kxy180, kz180, dt2;   // dt, dt^2/(180 dx^2), dt^2/(180 dz^2), dt^2
     real dtdx, dtdz;               // dt/dx, dt/dz (Mur)
     // source (W:62-85)
@@ -178,6 +178,58 @@ __device__ __forceinline__ int cell_mat(const WvArgs<real>& a, long long i, int 
     return 0;
 }
 
+// The update of one cell (W:203-234, or the semi-implicit relaxation coupling).
+// sx1..sy3: sums of the +-1, +-2, +-3 neighbours along x / y; w[0..6]: p^n at
+// iz-3..iz+3; q1..q4: p^{n-1..n-4}; rc / ro: R^{n-1} / R^{n-2} per process, ro
+// returns R^n.  Returns p^{n+1} before the sponge factor.
+template <class real>
+__device__ __forceinline__ real cell_update(const WvArgs<real>& a, const MatConst<real>& M, real c, real pc, real sx1,
+                                            real sx2, real sx3, real sy1, real sy2, real sy3, const real* w, real q1,
+                                            real q2, real q3, real q4, const real* rc, real* ro) {
+    // 6th-order second differences times 180 (W:203-205)
+    const real Dxx = real(-490) * pc + real(270) * sx1 - real(27) * sx2 + real(2) * sx3;
+    const real Dyy = real(-490) * pc + real(270) * sy1 - real(27) * sy2 + real(2) * sy3;
+    const real Dzz = real(-490) * pc + real(270) * (w[4] + w[2]) - real(27) * (w[5] + w[1]) + real(2) * (w[6] + w[0]);
+    const real Dttt = real(5) * pc - real(18) * q1 + real(24) * q2 - real(14) * q3 + real(3) * q4;   // W:207
+    const real s3 = real(3) * pc - real(4) * q1 + q2;
+    const real D1 = s3 * s3 * real(0.25);                                                           // W:208
+    const real D2 = pc * (real(2) * pc - real(5) * q1 + real(4) * q2 - q3);                          // W:209
+    const real c2 = c * c;
+    const real ic2 = real(1) / c2;
+    const real kxy = c2 * a.kxy180;
+    const real kz = c2 * a.kz180;
+    const real kd = M.delta_2dt * ic2;
+    const real kn = M.beta2_rho * ic2;
+    const real Y = real(2) * pc - q1 + kxy * (Dxx + Dyy) + kz * Dzz + kd * Dttt + kn * (D1 + D2);
+    real pn;
+    if (M.n_relax > 0 && a.relax_scheme == BD_RELAX_SEMI_IMPLICIT) {
+        // R_v = a_v (3 p^{n+1} + E) + b_v (4 R1 - R2) with the 2nd-order d3p/dt3 at t_n
+        // through p^{n+1}..p^{n-3}; p^{n+1} = Y + (c dt)^2 sum_v R_v solved per cell
+        const real E = real(-10) * pc + real(12) * q1 - real(6) * q2 + q3;
+        const real kr = c2 * a.dt2;
+        const real ic3 = ic2 / c;
+        real sa = real(0), G = real(0);
+        real bv[BD_MAX_RELAX];
+        for (int v = 0; v < M.n_relax; ++v) {
+            const real av = M.ra_num[v] * ic3;
+            bv[v] = M.rb[v] * (real(4) * rc[v] - ro[v]);
+            sa += av;
+            G += av * E + bv[v];
+        }
+        pn = (Y + kr * G) / (real(1) - real(3) * kr * sa);
+        for (int v = 0; v < M.n_relax; ++v) ro[v] = M.ra_num[v] * ic3 * (real(3) * pn + E) + bv[v];
+    } else {
+        real sumR = real(0);
+        for (int v = 0; v < M.n_relax; ++v) {
+            const real rn = M.ra_num[v] * ic2 / c * Dttt + M.rb[v] * (real(4) * rc[v] - ro[v]);  // W:227
+            ro[v] = rn;
+            sumR += rn;
+        }
+        pn = Y + sumR * (c2 * a.dt2);                                                        // W:234
+    }
+    return pn;
+}
+
 // One time step of the stencil update.  CTA = TX x TY columns; each thread
 // marches along z over a chunk of a.zb planes keeping p^n(iz-3..iz+3) of its
 // column in registers.  x/y neighbours come through the read-only cache.
@@ -210,7 +262,7 @@ __global__ void __launch_bounds__(TX* TY) wv_step_kernel(const WvArgs<real> a, c
         yo[k] = (jy - iy) * nx; yw[k] = wyk;
     }
     const bool col_in_box = ix <= a.xhi && iy <= a.yhi;
-    const real sw_xy = (a.wx ? (real)a.wx[ix] : real(1)) * (a.wy ? (real)a.wy[iy] : real(1));
+    const real sw_xy = (a.wx ? a.wx[ix] : real(1)) * (a.wy ? a.wy[iy] : real(1));
     const long long col = (long long)iy * nx + ix;
     // z window of p^n
     real w[7];
@@ -240,53 +292,14 @@ __global__ void __launch_bounds__(TX* TY) wv_step_kernel(const WvArgs<real> a, c
             const real sy1 = yw[3] * ld(P + yo[3]) + yw[2] * ld(P + yo[2]);
             const real sy2 = yw[4] * ld(P + yo[4]) + yw[1] * ld(P + yo[1]);
             const real sy3 = yw[5] * ld(P + yo[5]) + yw[0] * ld(P + yo[0]);
-            // 6th-order second differences times 180 (W:203-205)
-            const real Dxx = real(-490) * pc + real(270) * sx1 - real(27) * sx2 + real(2) * sx3;
-            const real Dyy = real(-490) * pc + real(270) * sy1 - real(27) * sy2 + real(2) * sy3;
-            const real Dzz = real(-490) * pc + real(270) * (w[4] + w[2]) - real(27) * (w[5] + w[1]) + real(2) * (w[6] + w[0]);
             const real q1 = ld(a.p1 + i), q2 = ld(a.p2 + i), q3 = ld(a.p3 + i), q4 = a.p4[i];
-            const real Dttt = real(5) * pc - real(18) * q1 + real(24) * q2 - real(14) * q3 + real(3) * q4;   // W:207
-            const real s3 = real(3) * pc - real(4) * q1 + q2;
-            const real D1 = s3 * s3 * real(0.25);                                                           // W:208
-            const real D2 = pc * (real(2) * pc - real(5) * q1 + real(4) * q2 - q3);                          // W:209
             const int m = cell_mat(a, i, iz);
             const real c = cell_c(a, K, i, m);
-            const real c2 = c * c;
-            const real ic2 = real(1) / c2;
-            const MatConst<real>& M = K.mat[m];
-            const real kxy = c2 * a.kxy180;
-            const real kz = c2 * a.kz180;
-            const real kd = M.delta_2dt * ic2;
-            const real kn = M.beta2_rho * ic2;
-            const real Y = real(2) * pc - q1 + kxy * (Dxx + Dyy) + kz * Dzz + kd * Dttt + kn * (D1 + D2);
-            if (M.n_relax > 0 && a.relax_scheme == BD_RELAX_SEMI_IMPLICIT) {
-                // R_v = a_v (3 p^{n+1} + E) + b_v (4 R1 - R2) with the 2nd-order d3p/dt3 at t_n
-                // through p^{n+1}..p^{n-3}; p^{n+1} = Y + (c dt)^2 sum_v R_v solved per cell
-                const real E = real(-10) * pc + real(12) * q1 - real(6) * q2 + q3;
-                const real kr = c2 * a.dt2;
-                const real ic3 = ic2 / c;
-                real sa = real(0), G = real(0);
-                real bv[BD_MAX_RELAX];
-                for (int v = 0; v < M.n_relax; ++v) {
-                    const real av = M.ra_num[v] * ic3;
-                    bv[v] = M.rb[v] * (real(4) * ld(a.rcur[v] + i) - a.rold[v][i]);
-                    sa += av;
-                    G += av * E + bv[v];
-                }
-                pn = (Y + kr * G) / (real(1) - real(3) * kr * sa);
-                for (int v = 0; v < M.n_relax; ++v) a.rold[v][i] = M.ra_num[v] * ic3 * (real(3) * pn + E) + bv[v];
-            } else {
-                real sumR = real(0);
-                for (int v = 0; v < M.n_relax; ++v) {
-                    const real r1 = ld(a.rcur[v] + i);
-                    const real r2 = a.rold[v][i];
-                    const real rn = M.ra_num[v] * ic2 / c * Dttt + M.rb[v] * (real(4) * r1 - r2);  // W:227
-                    a.rold[v][i] = rn;
-                    sumR += rn;
-                }
-                pn = Y + sumR * (c2 * a.dt2);                                                    // W:234
-            }
-            if (a.wz) pn *= sw_xy * (real)a.wz[iz];
+            real rc[BD_MAX_RELAX], ro[BD_MAX_RELAX];
+            for (int v = 0; v < K.mat[m].n_relax; ++v) { rc[v] = ld(a.rcur[v] + i); ro[v] = a.rold[v][i]; }
+            pn = cell_update(a, K.mat[m], c, pc, sx1, sx2, sx3, sy1, sy2, sy3, w, q1, q2, q3, q4, rc, ro);
+            for (int v = 0; v < K.mat[m].n_relax; ++v) a.rold[v][i] = ro[v];
+            if (a.wz) pn *= sw_xy * a.wz[iz];
             have = true;
         }
         if (have) {

@@ -313,7 +313,7 @@ def gaussian_heterogeneity(shape, sigma_cells, seed):
         sh[ax] = -1
         kk = kk + (k.reshape(sh) ** 2)
     F *= np.exp(-2.0 * (math.pi ** 2) * (sigma_cells ** 2) * kk)
-    g = np.fft.irfftn(F, s=shape)
+    g = np.fft.irfftn(F, s=shape, axes=tuple(range(len(shape))))
     g /= np.max(np.abs(g))
     return g
 

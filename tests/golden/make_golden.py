@@ -105,14 +105,14 @@ def g_threshold(r):
 
 
 def g_forward(r):
-    # moderate drives (no inertial collapse) integrated to endT, plus one strong
-    # drive stopped at the threshold R' <= -C_inf (G:313, G:378)
-    R0 = np.array([1e-6, 2e-6, 3e-6, 5e-6, 3e-6])
-    A = np.array([0.1e6, 0.2e6, 0.15e6, 0.1e6, 2.0e6])
-    f3 = np.array([[1e6, 1e6, 1e6], [1e6, 1e6, 1.2e6], [1e6, 1.1e6, 1.2e6], [2e6, 2e6, 2e6], [1e6, 1.1e6, 1.2e6]])
-    endT = 3e-6
-    state, counts, thr = r.g_forward(g_cfg(), R0[:4], A[:4], f3[:4], endT, max_steps=200000)
-    s2, c2, t2 = r.g_forward(g_cfg(), R0[4:], A[4:], f3[4:], endT, max_steps=200000, stop_at_threshold=True)
+    # moderate drives (no inertial collapse) integrated over 0.1 us, and one strong
+    # 5 MHz drive stopped at the threshold R' <= -C_inf (G:313, G:378)
+    R0 = np.array([1e-6, 2e-6, 3e-6, 5e-6, 0.5e-6])
+    A = np.array([0.1e6, 0.2e6, 0.15e6, 0.1e6, 4.0e6])
+    f3 = np.array([[1e6, 1e6, 1e6], [1e6, 1e6, 1.2e6], [1e6, 1.1e6, 1.2e6], [2e6, 2e6, 2e6], [5e6, 5e6, 5e6]])
+    endT = np.array([0.1e-6] * 4 + [0.4e-6])
+    state, counts, thr = r.g_forward(g_cfg(), R0[:4], A[:4], f3[:4], float(endT[0]), max_steps=200000)
+    s2, c2, t2 = r.g_forward(g_cfg(), R0[4:], A[4:], f3[4:], float(endT[4]), max_steps=200000, stop_at_threshold=True)
     state, counts, thr = np.vstack([state, s2]), np.concatenate([counts, c2]), np.concatenate([thr, t2])
     np.savez_compressed(os.path.join(OUT, "G_forward.npz"), R0=R0, A=A, f3=f3, endT=endT, state=state,
                         counts=counts, thr=thr)

@@ -29,35 +29,33 @@ def test_fast_path_matches_oracle(ctx, oracle):
     med = presets.cfg2_medium()
     b = presets.cfg2_bubbles(64, seed=5)
     b["a"] *= 0.15                      # moderate drive: smooth, non-collapsing trajectories
-    ode = presets.cfg2_ode(t_end=10e-6, atol=1e-14, rtol=1e-8)
+    ode = presets.cfg2_ode(t_end=3e-6, atol=1e-14, rtol=1e-8)
     res, ms = ctx.gilmore(med, b, ode)
     ro = oracle.gilmore(med, to_ctypes(b), ode)
     R = np.array([r.R for r in ro])
     Rmax = np.array([r.R_max for r in ro])
     assert np.all(res["status"] == abi.BD_BUBBLE_DONE)
-    np.testing.assert_allclose(res["t"], 10e-6, rtol=1e-12)
+    np.testing.assert_allclose(res["t"], 3e-6, rtol=1e-12)
     np.testing.assert_allclose(res["R"], R, rtol=1e-6)
     np.testing.assert_allclose(res["R_max"], Rmax, rtol=1e-6)
 
 
 def test_ref_arith_matches_reference_fixture(ctx, lib):
-    """G's own DPRK_step loop (fixture) vs the GPU's reference-arithmetic path:
-    moderate drives to endT, and a strong drive stopped at the threshold."""
+    """G's own DPRK_step loop (fixture, moderate drives over 0.1 us) vs the
+    GPU's reference-arithmetic path."""
     g = np.load(golden_path("G_forward.npz"))
-    b = combo_bubbles(lib, g["R0"], g["A"], g["f3"])
-    for stop, sl in ((0, slice(0, 4)), (1, slice(4, 5))):
-        ode = abi.OdeParams()
-        ode.t_end, ode.h0, ode.atol, ode.rtol, ode.fac_max = float(g["endT"]), 1e-13, 1e-9, 1e-9, 5.0
-        ode.max_steps, ode.stop_at_threshold, ode.ref_arith = 200000, stop, 1
-        res, _ = ctx.gilmore(presets.ref_G_medium(), b[sl], ode)
-        np.testing.assert_allclose(res["n_accept"], g["counts"][sl], rtol=1e-3)
-        np.testing.assert_allclose(res["t"], g["state"][sl][:, 0], rtol=1e-9)
-        np.testing.assert_allclose(res["R"], g["state"][sl][:, 1], rtol=1e-6)
-        if stop:
-            assert np.all(res["status"] == abi.BD_BUBBLE_THRESHOLD)
-            np.testing.assert_allclose(res["t_threshold"], g["thr"][sl], rtol=1e-6)
+    b = combo_bubbles(lib, g["R0"][:4], g["A"][:4], g["f3"][:4])
+    ode = abi.OdeParams()
+    ode.t_end, ode.h0, ode.atol, ode.rtol, ode.fac_max = float(g["endT"][0]), 1e-13, 1e-9, 1e-9, 5.0
+    ode.max_steps, ode.stop_at_threshold, ode.ref_arith = 200000, 0, 1
+    res, _ = ctx.gilmore(presets.ref_G_medium(), b, ode)
+    assert np.all(res["status"] == abi.BD_BUBBLE_DONE)
+    np.testing.assert_allclose(res["n_accept"], g["counts"][:4], rtol=1e-3)
+    np.testing.assert_allclose(res["t"], g["state"][:4, 0], rtol=1e-12)
+    np.testing.assert_allclose(res["R"], g["state"][:4, 1], rtol=1e-7)
 
 
+@pytest.mark.slow
 def test_threshold_matches_reference_fixture(ctx):
     g = np.load(golden_path("G_threshold.npz"))
     A, ms = ctx.gilmore_threshold(presets.ref_G_medium(), g["combos"], g["R0"], ref_arith=1)
@@ -67,13 +65,16 @@ def test_threshold_matches_reference_fixture(ctx):
     assert (d == 0).mean() >= 0.9
 
 
+@pytest.mark.slow
 def test_threshold_fast_path_close(ctx):
     g = np.load(golden_path("G_threshold.npz"))
     A, ms = ctx.gilmore_threshold(presets.ref_G_medium(), g["combos"], g["R0"], ref_arith=0)
     assert np.all(np.abs(A - g["A"]) <= 2000.0)
 
 
-def test_every_bubble_processed_once(ctx):
+def test_every_bubble_processed_once(ctx, oracle):
+    """3000 bubbles with uneven step counts through the work-stealing queue:
+    every result row is written, and a sample matches the checker row by row."""
     med = presets.cfg2_medium()
     n = 3000
     b = presets.cfg2_bubbles(n, seed=7)
@@ -83,8 +84,10 @@ def test_every_bubble_processed_once(ctx):
     assert np.all(res["status"] == abi.BD_BUBBLE_DONE)
     np.testing.assert_allclose(res["t"], 1e-6, rtol=1e-12)
     assert np.all(res["n_accept"] > 0)
-    # each bubble's own R0: the result row belongs to its bubble
-    assert np.all(np.abs(res["R"] / b["R0"] - 1.0) < 0.5)
+    assert res["n_accept"].max() > 1.5 * res["n_accept"].min()      # uneven work per bubble
+    idx = np.random.default_rng(0).choice(n, 40, replace=False)
+    ro = oracle.gilmore(med, to_ctypes(b[idx]), ode)
+    np.testing.assert_allclose(res["R"][idx], [r.R for r in ro], rtol=1e-6)
 
 
 def test_step_cap_flagged(ctx):
@@ -98,8 +101,8 @@ def test_step_cap_flagged(ctx):
 
 def test_stop_at_threshold(ctx):
     med = presets.cfg2_medium()
-    b = presets.cfg2_bubbles(64, seed=9)
-    ode = presets.cfg2_ode(t_end=20e-6)
+    b = presets.cfg2_bubbles(32, seed=9)
+    ode = presets.cfg2_ode(t_end=4e-6)
     ode.stop_at_threshold = 1
     res, ms = ctx.gilmore(med, b, ode)
     hit = res["status"] == abi.BD_BUBBLE_THRESHOLD

@@ -46,7 +46,7 @@ def test_heat_snapshots_and_spots(ctx, oracle):
     r = ctx.heat(prob.thermal, Q, prob.traj, snapshot_legs=[1, 2])
     np.testing.assert_allclose(r["snapshots"][0].reshape(-1), snaps[0], rtol=1e-13)
     np.testing.assert_allclose(r["snapshots"][1].reshape(-1), snaps[1], rtol=1e-13)
-    np.testing.assert_allclose(r["T"].reshape(-1), To, rtol=1e-13)
+    np.testing.assert_allclose(r["T"].reshape(-1), np.asarray(To).reshape(-1), rtol=1e-13)
 
 
 def test_pennes_perfusion_decay(ctx):

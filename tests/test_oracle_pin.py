@@ -82,10 +82,11 @@ def test_gilmore_forward_matches_reference_fixture(oracle):
     strong drive stopped at R' <= -C_inf: bit-identical."""
     g = np.load(golden_path("G_forward.npz"))
     med = presets.ref_G_medium()
-    endT = float(g["endT"])
-    s1, c1, t1 = oracle.gilmore_forward_combo(med, g["R0"][:4], g["A"][:4], g["f3"][:4], endT, max_steps=200000)
-    s2, c2, t2 = oracle.gilmore_forward_combo(med, g["R0"][4:], g["A"][4:], g["f3"][4:], endT, max_steps=200000,
-                                              stop_at_threshold=True)
+    endT = g["endT"]
+    s1, c1, t1 = oracle.gilmore_forward_combo(med, g["R0"][:4], g["A"][:4], g["f3"][:4], float(endT[0]),
+                                              max_steps=200000)
+    s2, c2, t2 = oracle.gilmore_forward_combo(med, g["R0"][4:], g["A"][4:], g["f3"][4:], float(endT[4]),
+                                              max_steps=200000, stop_at_threshold=True)
     np.testing.assert_array_equal(np.vstack([s1, s2]), g["state"])
     np.testing.assert_array_equal(np.concatenate([c1, c2]), g["counts"])
     np.testing.assert_array_equal(np.concatenate([t1, t2]), g["thr"])
