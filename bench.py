@@ -1,0 +1,299 @@
+"""Benchmark of the focused-ultrasound hot path (one JSON line on stdout).
+
+Default workload: the plain FP32 Westervelt configuration (128x128x256 cells,
+dx = 0.1875 mm, heterogeneous c, one relaxation process, 20-cell sponge, 1 MHz
+10-cycle bowl burst, 3000 time steps).  One benchmark step = one complete
+3000-time-step solve.  Metric: Westervelt Gcell-updates/s.
+
+  value      K solves on K sessions whose inputs are already on the device,
+             timed with CUDA events on the library's stream
+  e2e        K calls of bd_westervelt_run through the C ABI with host buffers:
+             c map and source tables uploaded, peak and energy maps read back
+  roofline   algorithmic bytes of the step kernel (56 B/cell) / its event-timed
+             duration, against the measured HBM copy bandwidth
+  cpu_baseline  the CPU checker (OpenMP, all host cores) on a bounded sample
+
+--impl reference times the reference's own Westervelt kernels built for the
+host (oracle/_ref) on the same grid (its two-layer physics), all host cores.
+--gpus N under torchrun: N independent replicas (the solver does not shard).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+CFG1 = dict(nx=128, ny=128, nz=256, n_steps=3000)
+BYTES_PER_CELL = 56          # p^n..p^{n-4} 20 B, p^{n+1} 4, R 12, c 4, peak 8, energy 8
+METRIC = "Westervelt Gcell-updates/s"
+UNIT = "Gcell-updates/s"
+# dram__bytes_read.sum + dram__bytes_write.sum of one wv_tma_kernel launch on the
+# cfg1 grid (ncu capture of the TMA step kernel; summary in profiles/)
+NCU_TRAFFIC_BYTES = 203990272
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for l in self.lines:
+            p = [x.strip() for x in l.split(",")]
+            if len(p) < 8:
+                continue
+            try:
+                sm.append(float(p[0]))
+                smax.append(float(p[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    return world, rank, local
+
+
+def dist_max(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def dist_barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def cfg1_problem(precision=None):
+    from bubbledynamics_gb300 import abi, presets
+    return presets.cfg1(CFG1["nx"], CFG1["ny"], CFG1["nz"], CFG1["n_steps"],
+                        precision=abi.BD_F32 if precision is None else precision)
+
+
+def cpu_baseline_port(sample_steps):
+    """The CPU checker on cfg1's grid for a few time steps, all host cores."""
+    from bubbledynamics_gb300 import abi, presets
+    from oracle.oracle import Oracle
+    o = Oracle()
+    p = presets.cfg1(CFG1["nx"], CFG1["ny"], CFG1["nz"], sample_steps, precision=abi.BD_F64)
+    t = time.perf_counter()
+    o.westervelt(p, want=("peak",))
+    dt = time.perf_counter() - t
+    cells = CFG1["nx"] * CFG1["ny"] * CFG1["nz"] * sample_steps
+    return {"value": cells / dt / 1e9, "unit": UNIT, "cores": o.threads(), "kind": "port",
+            "sample": "%d time steps of the 128x128x256 grid (FP64 checker, OpenMP), %.1f s" % (sample_steps, dt)}
+
+
+def reference_cpu(sample_steps):
+    """The reference's own Westervelt kernels (W:62-236) built for the host,
+    on a 128x128x256 grid with the reference's two-layer physics."""
+    from bubbledynamics_gb300 import presets
+    from oracle.oracle import RefLib
+    k = presets.ref_W_constants()
+    k["Nxy"] = CFG1["nx"]
+    k["Nz"] = CFG1["nz"]
+    r = RefLib()
+    t = time.perf_counter()
+    r.w_steps(k, sample_steps)
+    dt = time.perf_counter() - t
+    cells = CFG1["nx"] * CFG1["nx"] * CFG1["nz"] * sample_steps
+    return cells / dt / 1e9, dt
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    import multiprocessing
+    cores = multiprocessing.cpu_count()
+    try:
+        from oracle import build as ob
+        if ob.build_ref() is None:
+            raise FileNotFoundError("reference kernel sections not available")
+        kind = "reference"
+        sample = 6
+        for _ in range(args.warmup):
+            reference_cpu(1)
+        vals = []
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            v, dt = reference_cpu(sample)
+            vals.append(v)
+        wall = time.perf_counter() - t0
+        value = statistics.median(vals)
+        desc = ("%d time steps of W's Westervelt_space6 + source + Mur kernels and the 9-copy rotation "
+                "(W:139-236, W:62-135, W:575-584) on a 128x128x256 grid, host build, OpenMP over blocks" % sample)
+    except Exception as e:  # the reference build is unavailable: time the checker port instead
+        kind = "port"
+        cb = cpu_baseline_port(6)
+        value = cb["value"]
+        wall = 0.0
+        desc = "checker port (reference build unavailable: %s)" % str(e).splitlines()[0]
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": wall * 1e3 / max(args.steps, 1), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "westervelt 128x128x256 (reference two-layer physics, CPU)", "grid": [128, 128, 256]},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind, "sample": desc},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_westervelt(args, world, rank, local):
+    import torch
+    from bubbledynamics_gb300 import api
+    torch.cuda.set_device(local)
+    ctx = api.Context(local)
+    pk, pk_kind = peaks()
+    ncell = CFG1["nx"] * CFG1["ny"] * CFG1["nz"]
+    T = CFG1["n_steps"]
+    # ---- device-resident solves (value)
+    sessions = [ctx.westervelt_session(cfg1_problem()) for _ in range(args.warmup + args.steps)]
+    for s in sessions[: args.warmup]:
+        s.advance(T)
+    dist_barrier(world)
+    torch.cuda.synchronize()
+    l0 = ctx.kernel_launches()
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        dev_ms = []
+        for s in sessions[args.warmup:]:
+            s.advance(T)
+            dev_ms.append(s.last_ms())
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    launches = ctx.kernel_launches() - l0
+    dist_barrier(world)
+    total_ms = sum(dev_ms)
+    total_ms = dist_max(total_ms, world)
+    value = world * ncell * T * args.steps / (total_ms * 1e-3) / 1e9
+    for s in sessions:
+        s.close()
+    # ---- step kernel roofline: algorithmic bytes / event-timed step duration
+    step_us = total_ms * 1e3 / (args.steps * T)
+    achieved = BYTES_PER_CELL * ncell / (step_us * 1e-6) / 1e9
+    roof = {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
+            "frac": achieved / pk["hbm_gbs"], "traffic": NCU_TRAFFIC_BYTES,
+            "algorithmic_bytes": BYTES_PER_CELL * ncell, "peak_kind": pk_kind}
+    # ---- end to end through the C ABI with host buffers
+    prob = cfg1_problem()
+    cmap = prob.array("c_map")
+    h2d = cmap.nbytes + prob.grid.nx * prob.grid.ny * (4 + 4 * 4 + 4) + T * (8 + 16 + 4)
+    d2h = 2 * ncell * 4
+    ctx.westervelt(prob, want=("peak", "energy"))   # warm
+    dist_barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ctx.westervelt(prob, want=("peak", "energy"))
+    torch.cuda.synchronize()
+    e2e_s = dist_max(time.perf_counter() - t0, world)
+    e2e = {"value": world * ncell * T * args.steps / e2e_s / 1e9, "unit": UNIT,
+           "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)}
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_baseline_port(args.cpu_sample)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "cfg1 plain Westervelt FP32 128x128x256, 3000 time steps per step",
+                   "grid": [128, 128, 256], "time_steps_per_step": T, "dx_mm": 0.1875, "relax_processes": 1,
+                   "sponge_cells": 20, "parallelism": "replicas" if world > 1 else "single GPU",
+                   "l2": "inputs larger than L2 (about 170 MB of fields streamed per time step)"},
+        "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk.summary(),
+        "gpu_launches": int(launches),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="westervelt", choices=["westervelt"])
+    ap.add_argument("--cpu-sample", type=int, default=60)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_westervelt(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()
