@@ -74,6 +74,7 @@ def load(path=None):
     _sig(L, "bd_gilmore_run_device", [P, P, C.c_int64, P, P, P, P])
     _sig(L, "bd_gilmore_threshold", [P, P, P, C.c_int64, P, C.c_int64, C.c_int32, C.c_int64, P,
                                      C.POINTER(C.c_double)])
+    _sig(L, "bd_heat_run_device_noalloc", [P, P, P, P, P, P, C.c_int64, P])
     if hasattr(L, "bd_westervelt_adjoint"):
         _sig(L, "bd_westervelt_adjoint", [P, P, P, P, P, P, C.POINTER(C.c_double), P, P, P])
     _lib = L

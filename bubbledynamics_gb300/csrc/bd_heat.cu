@@ -13,6 +13,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "bd_internal.h"
@@ -105,6 +106,56 @@ __global__ void heat_step_kernel(const HeatArgs<real> a, int koff) {
 
 __global__ void heat_advance_kernel(long long* step_base, int n) {
     if (threadIdx.x == 0 && blockIdx.x == 0) *step_base += n;
+}
+
+// Coefficients of T:212-217 (plus the Pennes term) for each material.
+template <class real>
+static void heat_materials(const bd_thermal* th, double T_ref, HeatMat<real>* out) {
+    for (int k = 0; k < th->n_materials; ++k) {
+        const bd_thermal_material& mt = th->mat[k];
+        const double kk = mt.k_t / (mt.rho * mt.c_t);
+        const double kxy = th->dt * kk / (th->dx * th->dx), kz = th->dt * kk / (th->dz * th->dz);
+        const double w = mt.perfusion * th->dt;
+        out[k] = HeatMat<real>{(real)(1.0 - 4.0 * kxy - 2.0 * kz - w), (real)kxy, (real)kz,
+                               (real)(th->dt / (mt.rho * mt.c_t)), (real)(w * (mt.T_art - T_ref))};
+    }
+}
+
+// ----------------------------------------------------------------------------
+// Scratch of bd_heat_run_device_noalloc: one static device array, laid out as
+// [step counter: 256 B][plane materials][per-step shifts][second theta buffer].
+static __device__ __align__(256) unsigned char g_noalloc_scratch[BD_NOALLOC_SCRATCH_BYTES];
+
+struct NoallocScratch {
+    long long* step;
+    int* planemat;
+    int2* shifts;
+    float* theta;
+};
+
+static std::mutex g_noalloc_mu;
+static bool g_noalloc_ready[64];
+static unsigned char* g_noalloc_base[64];
+
+// Device address of the scratch array for the current device, looked up once
+// per device with that device current.
+static NoallocScratch noalloc_scratch(int dev) {
+    if (dev < 0 || dev >= 64) fail(BD_ERR_INVALID_ARG, "device %d out of range for the scratch table", dev);
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ready[dev]) {
+        unsigned char* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress((void**)&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p) fail(BD_ERR_CUDA, "cudaGetSymbolAddress of the scratch array failed: %s", cudaGetErrorString(e));
+        g_noalloc_base[dev] = p;
+        g_noalloc_ready[dev] = true;
+    }
+    unsigned char* b = g_noalloc_base[dev];
+    NoallocScratch s;
+    s.step = reinterpret_cast<long long*>(b);
+    s.planemat = reinterpret_cast<int*>(b + 256);
+    s.shifts = reinterpret_cast<int2*>(b + 256 + 4 * BD_NOALLOC_MAX_PLANES);
+    s.theta = reinterpret_cast<float*>(b + 256 + 4 * BD_NOALLOC_MAX_PLANES + 8 * BD_NOALLOC_MAX_STEPS);
+    return s;
 }
 
 }  // namespace bd
@@ -366,6 +417,70 @@ bd_status bd_spiral_heat_run(bd_context* ctx, const bd_thermal* th, const double
         }
         out->elapsed_ms = ms;
         out->steps_done = nsteps;
+    });
+}
+
+bd_status bd_heat_run_device_noalloc(bd_context* ctx, const bd_thermal* th, float* d_theta, const float* d_Q,
+                                     float* d_dose, const int32_t* shifts, int64_t n_steps, void* stream) {
+    return guard([&] {
+        ctx_check(ctx);
+        if (!th || !d_theta || !d_Q || !d_dose || (n_steps > 0 && !shifts)) fail(BD_ERR_INVALID_ARG, "null argument");
+        if (th->precision != BD_F32) fail(BD_ERR_INVALID_ARG, "the allocation-free heat run needs precision BD_F32");
+        if (th->material_map) fail(BD_ERR_UNSUPPORTED, "the allocation-free heat run takes plane_material only");
+        const int nx = th->nx, ny = th->ny, nz = th->nz;
+        if (nx < 3 || ny < 3 || nz < 3) fail(BD_ERR_INVALID_ARG, "grid too small");
+        const long long n = (long long)nx * ny * nz;
+        if (n > BD_NOALLOC_MAX_CELLS)
+            fail(BD_ERR_INVALID_ARG, "%lld cells exceed the allocation-free limit of %d", n, BD_NOALLOC_MAX_CELLS);
+        if (nz > BD_NOALLOC_MAX_PLANES)
+            fail(BD_ERR_INVALID_ARG, "%d planes exceed the allocation-free limit of %d", nz, BD_NOALLOC_MAX_PLANES);
+        if (n_steps < 0 || n_steps > BD_NOALLOC_MAX_STEPS)
+            fail(BD_ERR_INVALID_ARG, "%lld steps outside the allocation-free limit of %d", (long long)n_steps,
+                 BD_NOALLOC_MAX_STEPS);
+        if (th->n_materials < 1 || th->n_materials > BD_MAX_MATERIALS) fail(BD_ERR_INVALID_ARG, "n_materials out of range");
+        if (th->plane_material)
+            for (int iz = 0; iz < nz; ++iz)
+                if (th->plane_material[iz] < 0 || th->plane_material[iz] >= th->n_materials)
+                    fail(BD_ERR_INVALID_ARG, "plane_material entry out of range");
+        if (n_steps == 0) return;
+        const NoallocScratch sc = noalloc_scratch(ctx->device);
+        cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+        // the array keeps the last call's contents: the step counter restarts at zero,
+        // the partner buffer starts as a copy of the input field (faces are never written)
+        BD_CUDA(cudaMemsetAsync(sc.step, 0, sizeof(long long), s));
+        if (th->plane_material)
+            BD_CUDA(cudaMemcpyAsync(sc.planemat, th->plane_material, nz * sizeof(int), cudaMemcpyHostToDevice, s));
+        BD_CUDA(cudaMemcpyAsync(sc.shifts, shifts, (size_t)n_steps * sizeof(int2), cudaMemcpyHostToDevice, s));
+        BD_CUDA(cudaMemcpyAsync(sc.theta, d_theta, (size_t)n * sizeof(float), cudaMemcpyDeviceToDevice, s));
+        HeatArgs<float> a;
+        std::memset(&a, 0, sizeof a);
+        heat_materials<float>(th, th->T_ref, a.mat);
+        a.nx = nx; a.ny = ny; a.nz = nz; a.zb = 32; a.plane = (long long)nx * ny;
+        a.Q = d_Q;
+        a.TDf = reinterpret_cast<float2*>(d_dose);
+        a.plane_mat = th->plane_material ? sc.planemat : nullptr;
+        a.matmap = nullptr;
+        a.shifts = sc.shifts;
+        a.step_base = sc.step;
+        a.dt = (float)th->dt;
+        a.T_ref = th->T_ref;
+        a.T_refm43 = (float)(th->T_ref - 273.15 - 43.0);
+        dim3 block(32, 8), grid((nx + 31) / 32, (ny + 7) / 8, (nz + a.zb - 1) / a.zb);
+        const int CH = 64;
+        for (int64_t s0 = 0; s0 < n_steps; s0 += CH) {
+            const int cnt = (int)std::min<int64_t>(CH, n_steps - s0);
+            for (int k = 0; k < cnt; ++k) {
+                const bool even = ((s0 + k) % 2) == 0;   // even steps read the caller's field
+                a.Tin = even ? d_theta : sc.theta;
+                a.Tout = even ? sc.theta : d_theta;
+                heat_step_kernel<float><<<grid, block, 0, s>>>(a, k);
+                BD_LAUNCHED(ctx);
+            }
+            heat_advance_kernel<<<1, 32, 0, s>>>(sc.step, cnt);
+            BD_LAUNCHED(ctx);
+        }
+        if (n_steps % 2 == 1)   // the latest field is in the partner buffer
+            BD_CUDA(cudaMemcpyAsync(d_theta, sc.theta, (size_t)n * sizeof(float), cudaMemcpyDeviceToDevice, s));
     });
 }
 

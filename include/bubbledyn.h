@@ -322,6 +322,38 @@ bd_status bd_spiral_heat_run(bd_context* ctx, const bd_thermal* thermal, const d
                              const bd_trajectory* traj, int64_t max_steps,
                              bd_heat_outputs* out);
 
+/* Allocation-free variant of the FP32 heat + dose run, for callers that
+ * cannot call cudaMalloc: code running inside another framework's memory
+ * arena, which owns the device memory and forbids driver allocations, or a
+ * real-time loop where an allocation's implicit device synchronisation would
+ * stall other work.  No counterpart in the reference (whose host program
+ * allocates every field itself, T:259-306).
+ *
+ * The caller owns every input and output on the device: d_theta (nx*ny*nz
+ * floats, T - thermal->T_ref, updated in place), d_Q (nx*ny*nz floats, W/m^3)
+ * and d_dose (2*nx*ny*nz floats: hi, lo pairs whose sum is the CEM43 dose in
+ * seconds, updated in place).  shifts is a host array of n_steps (sx, sy)
+ * int32 pairs, e.g. from bd_trajectory_shifts.  The library's scratch (the
+ * second temperature buffer, the shift table and a step counter) is one
+ * static device array of BD_NOALLOC_SCRATCH_BYTES that every GPU which loads
+ * the library keeps until the process exits; sizes above BD_NOALLOC_MAX_CELLS
+ * cells, BD_NOALLOC_MAX_STEPS steps or BD_NOALLOC_MAX_PLANES planes are
+ * rejected with BD_ERR_INVALID_ARG.  thermal->precision must be BD_F32 and
+ * thermal->material_map NULL (plane_material is honoured).
+ *
+ * The first call on a device looks up the address of that array (with the
+ * device current); make that first call before any stream capture.  Every
+ * call shares the array and leaves its contents behind, so two calls whose
+ * work overlaps on the GPU (different streams, or different contexts on the
+ * same device) race with each other; serialise them.  The call returns once
+ * its work is enqueued on stream (NULL = the context's stream). */
+#define BD_NOALLOC_MAX_CELLS (1 << 21)
+#define BD_NOALLOC_MAX_STEPS (1 << 16)
+#define BD_NOALLOC_MAX_PLANES 4096
+#define BD_NOALLOC_SCRATCH_BYTES (256 + 4 * BD_NOALLOC_MAX_PLANES + 8 * BD_NOALLOC_MAX_STEPS + 4 * BD_NOALLOC_MAX_CELLS)
+bd_status bd_heat_run_device_noalloc(bd_context* ctx, const bd_thermal* thermal, float* d_theta, const float* d_Q,
+                                     float* d_dose, const int32_t* shifts, int64_t n_steps, void* stream);
+
 /* ------------------------------------------------------------------------- */
 /* Gilmore-Zener bubble dynamics (G)                                          */
 /* ------------------------------------------------------------------------- */
