@@ -37,7 +37,7 @@ static const Variant kVariants[] = {
     {32, 8, 32, 0}, {32, 4, 32, 0}, {64, 4, 32, 0}, {32, 8, 64, 0},
     {32, 16, 16, 0}, {64, 8, 16, 0}, {128, 2, 32, 0}, {32, 8, 0, 0},
     {32, 4, 32, 1}, {32, 8, 32, 1}, {64, 4, 32, 1}, {32, 4, 16, 1},
-    {32, 8, 16, 1}, {64, 4, 16, 1}, {32, 4, 64, 1}, {64, 2, 32, 1},
+    {32, 8, 16, 1}, {64, 4, 16, 1}, {32, 4, 64, 1}, {32, 8, 32, 1},
 };
 static const int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
@@ -205,9 +205,24 @@ static void build_maps(WvSession& S, int tx, int ty) {
     S.maps_ty = ty;
 }
 
-template <class real, int TX, int TY>
+template <class real, int TX, int TY, int CPT, int NREL>
+static void launch_tma_k(WvSession& S, const WvArgs<real>& a, const TmaMaps& maps, int koff, cudaStream_t st) {
+    using L = TmaLayout<real, TX, TY, (NREL >= 0 ? NREL : BD_MAX_RELAX)>;
+    static bool attr_done = false;
+    if (!attr_done) {
+        BD_CUDA(cudaFuncSetAttribute(wv_tma_kernel<real, TX, TY, CPT, NREL>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        attr_done = true;
+    }
+    dim3 block(TX, TY / CPT, 1);
+    dim3 grid((S.nx + TX - 1) / TX, (S.ny + TY - 1) / TY, (S.nz + a.zb - 1) / a.zb);
+    wv_tma_kernel<real, TX, TY, CPT, NREL><<<grid, block, L::SMEM, st>>>(a, S.kconst.as<WvConst<real>>(), koff, maps,
+                                                                         S.flag.as<unsigned>() + 1);
+    BD_LAUNCHED(S.ctx);
+}
+
+template <class real, int TX, int TY, int CPT>
 static void launch_tma_t(WvSession& S, const WvArgs<real>& a, int64_t s, int koff, cudaStream_t st) {
-    using L = TmaLayout<real, TX, TY>;
     build_maps(S, TX, TY);
     TmaMaps maps;
     std::memset(&maps, 0, sizeof maps);
@@ -219,18 +234,12 @@ static void launch_tma_t(WvSession& S, const WvArgs<real>& a, int64_t s, int kof
     maps.peak = S.mPeak;
     maps.energy = S.mEnergy;
     if (S.has_cmap) maps.cmap = S.mC;
-    const int smem = L::smem(S.max_relax, S.has_cmap);
-    static bool attr_set[2][64][64] = {};
-    bool& done = attr_set[sizeof(real) == 8][TX % 64][TY % 64];
-    if (!done) {
-        BD_CUDA(cudaFuncSetAttribute(wv_tma_kernel<real, TX, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-        done = true;
-    }
-    dim3 block(TX, TY, 1);
-    dim3 grid((S.nx + TX - 1) / TX, (S.ny + TY - 1) / TY, (S.nz + a.zb - 1) / a.zb);
-    wv_tma_kernel<real, TX, TY><<<grid, block, smem, st>>>(a, S.kconst.as<WvConst<real>>(), koff, maps,
-                                                            S.flag.as<unsigned>() + 1);
-    BD_LAUNCHED(S.ctx);
+    // FP32 kernels with 0, 1 or 2 relaxation processes are compiled for their count;
+    // FP64 and larger counts use the kernel that reads the count at run time
+    if (sizeof(real) == 4 && S.max_relax == 0) launch_tma_k<real, TX, TY, CPT, 0>(S, a, maps, koff, st);
+    else if (sizeof(real) == 4 && S.max_relax == 1) launch_tma_k<real, TX, TY, CPT, 1>(S, a, maps, koff, st);
+    else if (sizeof(real) == 4 && S.max_relax == 2) launch_tma_k<real, TX, TY, CPT, 2>(S, a, maps, koff, st);
+    else launch_tma_k<real, TX, TY, CPT, -1>(S, a, maps, koff, st);
 }
 
 template <class real, int TX, int TY>
@@ -254,10 +263,10 @@ static void launch_step(WvSession& S, int variant, int64_t s, int koff, cudaStre
         case 4: launch_step_t<real, 32, 16>(S, a, koff, st); break;
         case 5: launch_step_t<real, 64, 8>(S, a, koff, st); break;
         case 6: launch_step_t<real, 128, 2>(S, a, koff, st); break;
-        case 8: case 11: case 14: launch_tma_t<real, 32, 4>(S, a, s, koff, st); break;
-        case 9: case 12: launch_tma_t<real, 32, 8>(S, a, s, koff, st); break;
-        case 10: case 13: launch_tma_t<real, 64, 4>(S, a, s, koff, st); break;
-        case 15: launch_tma_t<real, 64, 2>(S, a, s, koff, st); break;
+        case 8: case 11: case 14: launch_tma_t<real, 32, 4, 1>(S, a, s, koff, st); break;
+        case 9: case 12: launch_tma_t<real, 32, 8, 2>(S, a, s, koff, st); break;
+        case 10: case 13: launch_tma_t<real, 64, 4, 2>(S, a, s, koff, st); break;
+        case 15: launch_tma_t<real, 32, 8, 1>(S, a, s, koff, st); break;
         default: fail(BD_ERR_INVALID_ARG, "bad tile variant %d", variant);
     }
     if (S.any_mur) {

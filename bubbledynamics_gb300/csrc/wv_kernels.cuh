@@ -92,6 +92,17 @@ struct WvArgs {
     int relax_scheme;
 };
 
+// Explicitly rounded arithmetic: the compiler never re-contracts these, so
+// every kernel variant that calls cell_update() produces the same bits.
+__device__ __forceinline__ float fma_(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double fma_(double a, double b, double c) { return __fma_rn(a, b, c); }
+__device__ __forceinline__ float mul_(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float add_(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double add_(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float div_(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ double div_(double a, double b) { return __ddiv_rn(a, b); }
+
 template <class real>
 __device__ __forceinline__ real ld(const real* p) { return __ldg(p); }
 
@@ -125,14 +136,27 @@ __device__ __forceinline__ float source_value<float>(const WvArgs<float>& a, lon
     }
     float sum = 0.0f;
     for (int k = 0; k < a.n_tones; ++k)
-        sum += a.tampf[k] * sinf(a.theta[step * BD_MAX_TONES + k] + a.sPsi[(long long)k * a.plane + j]);
-    return A * sum;
+        sum = fma_(a.tampf[k], sinf(add_(a.theta[step * BD_MAX_TONES + k], a.sPsi[(long long)k * a.plane + j])), sum);
+    return mul_(A, sum);
 }
 
 template <class real>
 __device__ __forceinline__ bool is_mur_cell(const WvArgs<real>& a, int ix, int iy, int iz) {
     return (a.mur_yp && iy >= a.ny - a.L) || (a.mur_xp && ix >= a.nx - a.L) ||
            (a.mur_zp && iz >= a.nz - a.L) || (a.mur_zm && iz < a.Lzm);
+}
+
+// Energy accumulator update: E + p^2 dt, or E + ((p^{n+1}-p^{n-1})/2dt)^2 dt (W:253-257).
+template <class real>
+__device__ __forceinline__ real energy_add(const WvArgs<real>& a, real old, real v, real vm1) {
+    real e;
+    if (a.energy_mode == BD_ENERGY_DPDT2) {
+        const real dp = div_(add_(v, -vm1), mul_(real(2.0), a.dt));     // W:253
+        e = mul_(mul_(dp, dp), a.dt);                                    // W:257
+    } else {
+        e = mul_(mul_(v, v), a.dt);
+    }
+    return add_(old, e);
 }
 
 // Peak / energy / DFT accumulation on the final p^{n+1} of a cell.
@@ -144,24 +168,15 @@ __device__ __forceinline__ void accumulate(const WvArgs<real>& a, long long step
         const real pk = a.peak[i];
         a.peak[i] = av > pk ? av : pk;
     }
-    if (step >= a.energy_start && step < a.energy_end) {
-        real e;
-        if (a.energy_mode == BD_ENERGY_DPDT2) {
-            const real dp = (v - vm1) / (real(2.0) * a.dt);    // W:253
-            e = dp * dp * a.dt;                                 // W:257
-        } else {
-            e = v * v * a.dt;
-        }
-        a.energy[i] += e;
-    }
+    if (step >= a.energy_start && step < a.energy_end) a.energy[i] = energy_add(a, a.energy[i], v, vm1);
     const long long ds = step - a.dft_start;
     if (a.n_dft > 0 && ds >= 0 && ds < a.dft_len && iz >= a.dz_lo && iz < a.dz_hi) {
         const long long pl = (long long)(iz - a.dz_lo) * a.plane + (long long)iy * a.nx + ix;
         const long long stride = (long long)(a.dz_hi - a.dz_lo) * a.plane;
         const real* tw = a.tw + ds * a.n_dft * 2;
         for (int j = 0; j < a.n_dft; ++j) {
-            a.dre[j * stride + pl] += v * tw[2 * j];
-            a.dim[j * stride + pl] -= v * tw[2 * j + 1];
+            a.dre[j * stride + pl] = fma_(v, tw[2 * j], a.dre[j * stride + pl]);
+            a.dim[j * stride + pl] = fma_(-v, tw[2 * j + 1], a.dim[j * stride + pl]);
         }
     }
 }
@@ -178,54 +193,75 @@ __device__ __forceinline__ int cell_mat(const WvArgs<real>& a, long long i, int 
     return 0;
 }
 
+// 6th-order second difference times 180 (W:203-205): -490 p + 270 s1 - 27 s2 + 2 s3
+template <class real>
+__device__ __forceinline__ real d2x180(real pc, real s1, real s2, real s3) {
+    return fma_(real(2), s3, fma_(real(-27), s2, fma_(real(270), s1, mul_(real(-490), pc))));
+}
+
 // The update of one cell (W:203-234, or the semi-implicit relaxation coupling).
 // sx1..sy3: sums of the +-1, +-2, +-3 neighbours along x / y; w[0..6]: p^n at
 // iz-3..iz+3; q1..q4: p^{n-1..n-4}; rc / ro: R^{n-1} / R^{n-2} per process, ro
 // returns R^n.  Returns p^{n+1} before the sponge factor.
-template <class real>
+template <class real, int NRMAX = BD_MAX_RELAX>
 __device__ __forceinline__ real cell_update(const WvArgs<real>& a, const MatConst<real>& M, real c, real pc, real sx1,
                                             real sx2, real sx3, real sy1, real sy2, real sy3, const real* w, real q1,
                                             real q2, real q3, real q4, const real* rc, real* ro) {
-    // 6th-order second differences times 180 (W:203-205)
-    const real Dxx = real(-490) * pc + real(270) * sx1 - real(27) * sx2 + real(2) * sx3;
-    const real Dyy = real(-490) * pc + real(270) * sy1 - real(27) * sy2 + real(2) * sy3;
-    const real Dzz = real(-490) * pc + real(270) * (w[4] + w[2]) - real(27) * (w[5] + w[1]) + real(2) * (w[6] + w[0]);
-    const real Dttt = real(5) * pc - real(18) * q1 + real(24) * q2 - real(14) * q3 + real(3) * q4;   // W:207
-    const real s3 = real(3) * pc - real(4) * q1 + q2;
-    const real D1 = s3 * s3 * real(0.25);                                                           // W:208
-    const real D2 = pc * (real(2) * pc - real(5) * q1 + real(4) * q2 - q3);                          // W:209
-    const real c2 = c * c;
-    const real ic2 = real(1) / c2;
-    const real kxy = c2 * a.kxy180;
-    const real kz = c2 * a.kz180;
-    const real kd = M.delta_2dt * ic2;
-    const real kn = M.beta2_rho * ic2;
-    const real Y = real(2) * pc - q1 + kxy * (Dxx + Dyy) + kz * Dzz + kd * Dttt + kn * (D1 + D2);
+    const real Dxx = d2x180(pc, sx1, sx2, sx3);
+    const real Dyy = d2x180(pc, sy1, sy2, sy3);
+    const real Dzz = d2x180(pc, add_(w[4], w[2]), add_(w[5], w[1]), add_(w[6], w[0]));
+    // W:207: 5 p - 18 p1 + 24 p2 - 14 p3 + 3 p4
+    const real Dttt = fma_(real(3), q4, fma_(real(-14), q3, fma_(real(24), q2, fma_(real(-18), q1, mul_(real(5), pc)))));
+    const real s3 = fma_(real(3), pc, fma_(real(-4), q1, q2));
+    const real D1 = mul_(mul_(s3, s3), real(0.25));                                                   // W:208
+    const real D2 = mul_(pc, fma_(real(2), pc, fma_(real(-5), q1, fma_(real(4), q2, -q3))));          // W:209
+    const real c2 = mul_(c, c);
+    const real ic2 = div_(real(1), c2);
+    const real kxy = mul_(c2, a.kxy180);
+    const real kz = mul_(c2, a.kz180);
+    const real kd = mul_(M.delta_2dt, ic2);
+    const real kn = mul_(M.beta2_rho, ic2);
+    // W:234 without the relaxation term: 2p - p1 + kxy (Dxx + Dyy) + kz Dzz + kd Dttt + kn (D1 + D2)
+    real Y = fma_(real(2), pc, -q1);
+    Y = fma_(kxy, add_(Dxx, Dyy), Y);
+    Y = fma_(kz, Dzz, Y);
+    Y = fma_(kd, Dttt, Y);
+    Y = fma_(kn, add_(D1, D2), Y);
     real pn;
     if (M.n_relax > 0 && a.relax_scheme == BD_RELAX_SEMI_IMPLICIT) {
         // R_v = a_v (3 p^{n+1} + E) + b_v (4 R1 - R2) with the 2nd-order d3p/dt3 at t_n
         // through p^{n+1}..p^{n-3}; p^{n+1} = Y + (c dt)^2 sum_v R_v solved per cell
-        const real E = real(-10) * pc + real(12) * q1 - real(6) * q2 + q3;
-        const real kr = c2 * a.dt2;
-        const real ic3 = ic2 / c;
+        const real E = fma_(real(-10), pc, fma_(real(12), q1, fma_(real(-6), q2, q3)));
+        const real kr = mul_(c2, a.dt2);
+        const real ic3 = div_(ic2, c);
         real sa = real(0), G = real(0);
-        real bv[BD_MAX_RELAX];
-        for (int v = 0; v < M.n_relax; ++v) {
-            const real av = M.ra_num[v] * ic3;
-            bv[v] = M.rb[v] * (real(4) * rc[v] - ro[v]);
-            sa += av;
-            G += av * E + bv[v];
+        real av[NRMAX > 0 ? NRMAX : 1], bv[NRMAX > 0 ? NRMAX : 1];
+#pragma unroll
+        for (int v = 0; v < NRMAX; ++v) {
+            if (v < M.n_relax) {
+                av[v] = mul_(M.ra_num[v], ic3);
+                bv[v] = mul_(M.rb[v], fma_(real(4), rc[v], -ro[v]));
+                sa = add_(sa, av[v]);
+                G = add_(G, fma_(av[v], E, bv[v]));
+            }
         }
-        pn = (Y + kr * G) / (real(1) - real(3) * kr * sa);
-        for (int v = 0; v < M.n_relax; ++v) ro[v] = M.ra_num[v] * ic3 * (real(3) * pn + E) + bv[v];
+        pn = div_(fma_(kr, G, Y), fma_(mul_(real(-3), kr), sa, real(1)));
+#pragma unroll
+        for (int v = 0; v < NRMAX; ++v)
+            if (v < M.n_relax) ro[v] = fma_(av[v], fma_(real(3), pn, E), bv[v]);
     } else {
         real sumR = real(0);
-        for (int v = 0; v < M.n_relax; ++v) {
-            const real rn = M.ra_num[v] * ic2 / c * Dttt + M.rb[v] * (real(4) * rc[v] - ro[v]);  // W:227
-            ro[v] = rn;
-            sumR += rn;
+#pragma unroll
+        for (int v = 0; v < NRMAX; ++v) {
+            if (v < M.n_relax) {
+                // W:227: R = 2dt 2 c_v tau Dttt/(2dt^3) / ((2dt+3tau) c^3) + tau (4 R1 - R2)/(2dt+3tau)
+                const real rn = fma_(mul_(mul_(M.ra_num[v], ic2), div_(real(1), c)), Dttt,
+                                     mul_(M.rb[v], fma_(real(4), rc[v], -ro[v])));
+                ro[v] = rn;
+                sumR = add_(sumR, rn);
+            }
         }
-        pn = Y + sumR * (c2 * a.dt2);                                                        // W:234
+        pn = fma_(sumR, mul_(c2, a.dt2), Y);                                                 // W:234
     }
     return pn;
 }
@@ -262,7 +298,7 @@ __global__ void __launch_bounds__(TX* TY) wv_step_kernel(const WvArgs<real> a, c
         yo[k] = (jy - iy) * nx; yw[k] = wyk;
     }
     const bool col_in_box = ix <= a.xhi && iy <= a.yhi;
-    const real sw_xy = (a.wx ? a.wx[ix] : real(1)) * (a.wy ? a.wy[iy] : real(1));
+    const real sw_xy = a.wx ? mul_(a.wx[ix], a.wy[iy]) : real(1);
     const long long col = (long long)iy * nx + ix;
     // z window of p^n
     real w[7];
@@ -299,7 +335,7 @@ __global__ void __launch_bounds__(TX* TY) wv_step_kernel(const WvArgs<real> a, c
             for (int v = 0; v < K.mat[m].n_relax; ++v) { rc[v] = ld(a.rcur[v] + i); ro[v] = a.rold[v][i]; }
             pn = cell_update(a, K.mat[m], c, pc, sx1, sx2, sx3, sy1, sy2, sy3, w, q1, q2, q3, q4, rc, ro);
             for (int v = 0; v < K.mat[m].n_relax; ++v) a.rold[v][i] = ro[v];
-            if (a.wz) pn *= sw_xy * a.wz[iz];
+            if (a.wz) pn = mul_(pn, mul_(sw_xy, a.wz[iz]));
             have = true;
         }
         if (have) {

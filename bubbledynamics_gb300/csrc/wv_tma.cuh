@@ -86,7 +86,9 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, u
         : "memory");
 }
 
-template <class real, int TX, int TY>
+// Shared-memory layout.  NRMAX is the number of relaxation processes the slot
+// has room for (the compile-time count, or BD_MAX_RELAX for the generic kernel).
+template <class real, int TX, int TY, int NRMAX>
 struct TmaLayout {
     static constexpr int PW = TX + 8, PH = TY + 6;
     static constexpr int PT = PW * PH;
@@ -94,38 +96,50 @@ struct TmaLayout {
     static constexpr int QT = TX * TY;
     static constexpr int QTB = QT * (int)sizeof(real);                            // bytes per real tile
     static constexpr int QTF = QT * 4;                                            // bytes of the float c tile
-    __host__ __device__ static int qslot(int nrel, bool has_c) { return (4 + 2 * nrel + 2) * QTB + (has_c ? QTF : 0); }
-    __host__ __device__ static int smem(int nrel, bool has_c) { return TMA_NP * PSLOT + TMA_NQ * qslot(nrel, has_c) + (TMA_NP + TMA_NQ) * 8; }
+    static constexpr int NQR = 4 + 2 * NRMAX + 2;                                 // real tiles per slot
+    static constexpr int QS = NQR * QTB + QTF;                                    // slot bytes
+    static constexpr int K_PEAK = 4 + 2 * NRMAX, K_ENERGY = 5 + 2 * NRMAX;
+    static constexpr int SMEM = TMA_NP * PSLOT + TMA_NQ * QS + (TMA_NP + TMA_NQ) * 8;
 };
 
-template <class real, int TX, int TY>
-__global__ void __launch_bounds__(TX* TY) wv_tma_kernel(const WvArgs<real> a, const WvConst<real>* __restrict__ Kp,
-                                                        int koff, const __grid_constant__ TmaMaps maps,
-                                                        unsigned* __restrict__ err) {
-    using L = TmaLayout<real, TX, TY>;
+// One Westervelt step, TMA-pipelined.  Template parameters: tile TX x TY, CPT
+// cells per thread along y (the CTA has TX x TY/CPT threads), NREL relaxation
+// processes known at compile time (-1: read from the arguments, up to
+// BD_MAX_RELAX).  The cell update is cell_update(), so every variant gives the
+// same bits as the plain kernel.
+template <class real, int TX, int TY, int CPT, int NREL>
+__global__ void __launch_bounds__(TX* TY / CPT) wv_tma_kernel(const WvArgs<real> a,
+                                                              const WvConst<real>* __restrict__ Kp, int koff,
+                                                              const __grid_constant__ TmaMaps maps,
+                                                              unsigned* __restrict__ err) {
+    constexpr int NRMAX = NREL >= 0 ? NREL : BD_MAX_RELAX;
+    using L = TmaLayout<real, TX, TY, NRMAX>;
+    constexpr int RPT = TY / CPT;                  // thread rows
+    constexpr int NT = TX * RPT;                   // threads
     extern __shared__ __align__(128) unsigned char smem[];
-    const int nrel = a.max_relax;
+    __shared__ MatConst<real> sK[BD_MAX_MATERIALS];
+    const int nrel = NREL >= 0 ? NREL : a.max_relax;
     const bool has_c = a.cmap != nullptr;
-    const int QS = L::qslot(nrel, has_c);
     real* Pring = reinterpret_cast<real*>(smem);
     unsigned char* Qring = smem + TMA_NP * L::PSLOT;
-    uint64_t* barP = reinterpret_cast<uint64_t*>(Qring + TMA_NQ * QS);
+    uint64_t* barP = reinterpret_cast<uint64_t*>(Qring + TMA_NQ * L::QS);
     uint64_t* barQ = barP + TMA_NP;
 
-    const int tx = threadIdx.x, ty = threadIdx.y;
-    const int tid = ty * TX + tx;
+    const int tx = threadIdx.x, tyt = threadIdx.y;
+    const int tid = tyt * TX + tx;
     const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
-    const int ix = x0 + tx, iy = y0 + ty;
-    const bool active = ix < a.nx && iy < a.ny;
     const int z0 = blockIdx.z * a.zb;
     const int z1 = min(a.nz, z0 + a.zb);
     const int zbn = z1 - z0;
     const long long step = *a.step_base + koff;
-    const WvConst<real>& K = *Kp;
 
-    auto pslot = [&](int q) { return reinterpret_cast<real*>(reinterpret_cast<unsigned char*>(Pring) + (q % TMA_NP) * L::PSLOT); };
-    auto qtile = [&](int r, int k) { return reinterpret_cast<real*>(Qring + (r % TMA_NQ) * QS + k * L::QTB); };
-    auto ctile = [&](int r) { return reinterpret_cast<float*>(Qring + (r % TMA_NQ) * QS + (4 + 2 * nrel + 2) * L::QTB); };
+    for (int e = tid; e < (int)(BD_MAX_MATERIALS * sizeof(MatConst<real>) / 4); e += NT)
+        reinterpret_cast<unsigned*>(sK)[e] = reinterpret_cast<const unsigned*>(Kp)[e];
+
+    auto pslot = [&](int q) {
+        return reinterpret_cast<real*>(reinterpret_cast<unsigned char*>(Pring) + (q % TMA_NP) * L::PSLOT);
+    };
+    auto qslot = [&](int r) { return Qring + (r % TMA_NQ) * L::QS; };
 
     // producer (thread 0): plane q = plane - (z0 - 3) of p^n, plane r = plane - z0 of the pointwise tiles
     auto issueP = [&](int q) {
@@ -140,15 +154,16 @@ __global__ void __launch_bounds__(TX* TY) wv_tma_kernel(const WvArgs<real> a, co
         if (r >= zbn) return;
         const int plane = z0 + r;
         uint64_t* bar = &barQ[r % TMA_NQ];
-        mbar_expect_tx(bar, (unsigned)QS);
-        for (int k = 0; k < 4; ++k) tma_load_3d(qtile(r, k), &maps.q[k], bar, x0, y0, plane);
+        unsigned char* q = qslot(r);
+        mbar_expect_tx(bar, (unsigned)((6 + 2 * nrel) * L::QTB + (has_c ? L::QTF : 0)));
+        for (int k = 0; k < 4; ++k) tma_load_3d(q + k * L::QTB, &maps.q[k], bar, x0, y0, plane);
         for (int v = 0; v < nrel; ++v) {
-            tma_load_3d(qtile(r, 4 + v), &maps.rc[v], bar, x0, y0, plane);
-            tma_load_3d(qtile(r, 4 + nrel + v), &maps.ro[v], bar, x0, y0, plane);
+            tma_load_3d(q + (4 + v) * L::QTB, &maps.rc[v], bar, x0, y0, plane);
+            tma_load_3d(q + (4 + NRMAX + v) * L::QTB, &maps.ro[v], bar, x0, y0, plane);
         }
-        tma_load_3d(qtile(r, 4 + 2 * nrel), &maps.peak, bar, x0, y0, plane);
-        tma_load_3d(qtile(r, 5 + 2 * nrel), &maps.energy, bar, x0, y0, plane);
-        if (has_c) tma_load_3d(ctile(r), &maps.cmap, bar, x0, y0, plane);
+        tma_load_3d(q + L::K_PEAK * L::QTB, &maps.peak, bar, x0, y0, plane);
+        tma_load_3d(q + L::K_ENERGY * L::QTB, &maps.energy, bar, x0, y0, plane);
+        if (has_c) tma_load_3d(q + L::NQR * L::QTB, &maps.cmap, bar, x0, y0, plane);
     };
 
     if (tid == 0) {
@@ -164,96 +179,131 @@ __global__ void __launch_bounds__(TX* TY) wv_tma_kernel(const WvArgs<real> a, co
     auto waitP = [&](int q) { mbar_wait(&barP[q % TMA_NP], (unsigned)((q / TMA_NP) & 1), err); };
     auto waitQ = [&](int r) { mbar_wait(&barQ[r % TMA_NQ], (unsigned)((r / TMA_NQ) & 1), err); };
 
-    const int own = (ty + 3) * L::PW + tx + 4;     // this column inside a plane tile
-    real w[7];
+    // per-cell constants of this thread's CPT cells (rows tyt, tyt + RPT, ...)
+    int own[CPT], qi[CPT];
+    bool active[CPT], inbox[CPT], murxy[CPT];
+    real swxy[CPT];
+    long long col[CPT];
+#pragma unroll
+    for (int c = 0; c < CPT; ++c) {
+        const int ty = tyt + c * RPT;
+        const int ix = x0 + tx, iy = y0 + ty;
+        own[c] = (ty + 3) * L::PW + tx + 4;
+        qi[c] = ty * TX + tx;
+        active[c] = ix < a.nx && iy < a.ny;
+        inbox[c] = ix <= a.xhi && iy <= a.yhi;
+        murxy[c] = (a.mur_yp && iy >= a.ny - a.L) || (a.mur_xp && ix >= a.nx - a.L);
+        swxy[c] = (a.wx && active[c]) ? mul_(a.wx[ix], a.wy[iy]) : real(1);
+        col[c] = (long long)iy * a.nx + ix;
+    }
+    real w[CPT][7];
     for (int k = 0; k < 6; ++k) {                  // planes z0-3 .. z0+2
         waitP(k);
         const int plane = z0 - 3 + k;
-        w[k] = (plane >= 0 && plane < a.nz) ? pslot(k)[own] : real(0);
+        const bool in = plane >= 0 && plane < a.nz;
+#pragma unroll
+        for (int c = 0; c < CPT; ++c) w[c][k] = in ? pslot(k)[own[c]] : real(0);
     }
     __syncthreads();                               // slots of planes z0-3..z0-1 are free again
     if (tid == 0)
         for (int q = TMA_NP; q < TMA_NP + 3; ++q) issueP(q);
 
-    const bool col_in_box = ix <= a.xhi && iy <= a.yhi;
-    const real sw_xy = (a.wx && active) ? a.wx[ix] * a.wy[iy] : real(1);
-    const long long col = (long long)iy * a.nx + ix;
     const bool fix_x = a.mir_x && x0 == 0, fix_y = a.mir_y && y0 == 0;
+    const bool do_peak = step >= a.peak_start && step < a.peak_end;
+    const bool do_energy = step >= a.energy_start && step < a.energy_end;
+    const long long ds = step - a.dft_start;
+    const bool do_dft = a.n_dft > 0 && ds >= 0 && ds < a.dft_len;
+    const bool single_mat = !a.matmap && !a.plane_mat;
 
     for (int iz = z0; iz < z1; ++iz) {
         const int qc = iz - z0 + 3;                // stencil plane
         const int r = iz - z0;
         waitP(qc + 3);
-        w[6] = (iz + 3 < a.nz) ? pslot(qc + 3)[own] : real(0);
+        {
+            const bool in = iz + 3 < a.nz;
+            const real* T6 = pslot(qc + 3);
+#pragma unroll
+            for (int c = 0; c < CPT; ++c) w[c][6] = in ? T6[own[c]] : real(0);
+        }
         real* T = pslot(qc);
         if (fix_x || fix_y) {                      // mirror planes x = 0 / y = 0 (W:176-200)
             if (fix_x)
-                for (int e = tid; e < L::PH * 3; e += TX * TY) {
+                for (int e = tid; e < L::PH * 3; e += NT) {
                     const int row = e / 3, k = e % 3 + 1;
                     T[row * L::PW + 4 - k] = T[row * L::PW + 4 + k];
                 }
             __syncthreads();
             if (fix_y)
-                for (int e = tid; e < L::PW * 3; e += TX * TY) {
-                    const int c = e % L::PW, k = e / L::PW + 1;
-                    T[(3 - k) * L::PW + c] = T[(3 + k) * L::PW + c];
+                for (int e = tid; e < L::PW * 3; e += NT) {
+                    const int cc = e % L::PW, k = e / L::PW + 1;
+                    T[(3 - k) * L::PW + cc] = T[(3 + k) * L::PW + cc];
                 }
             __syncthreads();
         }
         waitQ(r);
-        if (active) {
-            const long long i = (long long)iz * a.plane + col;
-            const int qi = ty * TX + tx;
-            const real q1 = qtile(r, 0)[qi];
-            const bool mur = is_mur_cell(a, ix, iy, iz);
+        const unsigned char* Qs = qslot(r);
+        const real* q1t = reinterpret_cast<const real*>(Qs);
+        const real* q2t = q1t + L::QT;
+        const real* q3t = q2t + L::QT;
+        const real* q4t = q3t + L::QT;
+        const real* pkt = reinterpret_cast<const real*>(Qs + L::K_PEAK * L::QTB);
+        const real* ent = reinterpret_cast<const real*>(Qs + L::K_ENERGY * L::QTB);
+        const float* ct = reinterpret_cast<const float*>(Qs + L::NQR * L::QTB);
+        const bool src_plane = iz == a.src_iz;
+        const bool zin = iz >= a.zlo && iz <= a.zhi && !src_plane;
+        const bool murz = (a.mur_zp && iz >= a.nz - a.L) || (a.mur_zm && iz < a.Lzm);
+        const real wzi = a.wz ? a.wz[iz] : real(1);
+        const int mplane = single_mat ? 0 : (a.plane_mat ? __ldg(a.plane_mat + iz) : 0);
+#pragma unroll
+        for (int c = 0; c < CPT; ++c) {
+            if (!active[c]) continue;
+            const long long i = (long long)iz * a.plane + col[c];
+            const int k = qi[c];
+            const real q1 = q1t[k];
             real pn;
             bool have = false;
-            real ro[BD_MAX_RELAX];
-            int m = 0;
-            if (iz == a.src_iz) {
-                pn = source_value<real>(a, step, (int)col);
+            if (src_plane) {
+                pn = source_value<real>(a, step, (int)col[c]);
                 have = true;
-            } else if (col_in_box && iz >= a.zlo && iz <= a.zhi) {
-                const real* c0 = T + own;
-                const real pc = w[3];
+            } else if (zin && inbox[c]) {
+                const real* c0 = T + own[c];
+                const real pc = w[c][3];
                 const real sx1 = c0[1] + c0[-1], sx2 = c0[2] + c0[-2], sx3 = c0[3] + c0[-3];
-                const int W = L::PW;
+                constexpr int W = L::PW;
                 const real sy1 = c0[W] + c0[-W], sy2 = c0[2 * W] + c0[-2 * W], sy3 = c0[3 * W] + c0[-3 * W];
-                m = cell_mat(a, i, iz);
-                const real c = has_c ? (real)ctile(r)[qi] : K.mat[m].c0;
-                real rc[BD_MAX_RELAX];
-                for (int v = 0; v < K.mat[m].n_relax; ++v) { rc[v] = qtile(r, 4 + v)[qi]; ro[v] = qtile(r, 4 + nrel + v)[qi]; }
-                pn = cell_update(a, K.mat[m], c, pc, sx1, sx2, sx3, sy1, sy2, sy3, w, q1, qtile(r, 1)[qi],
-                                 qtile(r, 2)[qi], qtile(r, 3)[qi], rc, ro);
-                for (int v = 0; v < K.mat[m].n_relax; ++v) a.rold[v][i] = ro[v];
-                if (a.wz) pn *= sw_xy * a.wz[iz];
+                const int m = a.matmap ? (int)__ldg(a.matmap + i) : mplane;
+                const MatConst<real>& M = sK[m];
+                const real cs = has_c ? (real)ct[k] : M.c0;
+                real rc[NRMAX > 0 ? NRMAX : 1], ro[NRMAX > 0 ? NRMAX : 1];
+#pragma unroll
+                for (int v = 0; v < NRMAX; ++v) {
+                    if (v < M.n_relax) {
+                        rc[v] = reinterpret_cast<const real*>(Qs + (4 + v) * L::QTB)[k];
+                        ro[v] = reinterpret_cast<const real*>(Qs + (4 + NRMAX + v) * L::QTB)[k];
+                    }
+                }
+                pn = cell_update<real, NRMAX>(a, M, cs, pc, sx1, sx2, sx3, sy1, sy2, sy3, w[c], q1, q2t[k], q3t[k], q4t[k], rc, ro);
+#pragma unroll
+                for (int v = 0; v < NRMAX; ++v)
+                    if (v < M.n_relax) a.rold[v][i] = ro[v];
+                if (a.wz) pn = mul_(pn, mul_(swxy[c], wzi));
                 have = true;
             }
             if (have) {
                 a.p4[i] = pn;
-                if (!mur) {
-                    if (step >= a.peak_start && step < a.peak_end) {
-                        const real av = fabs(pn), pk = qtile(r, 4 + 2 * nrel)[qi];
+                if (!(murz || murxy[c])) {
+                    if (do_peak) {
+                        const real av = fabs(pn), pk = pkt[k];
                         a.peak[i] = av > pk ? av : pk;
                     }
-                    if (step >= a.energy_start && step < a.energy_end) {
-                        real e;
-                        if (a.energy_mode == BD_ENERGY_DPDT2) {
-                            const real dp = (pn - q1) / (real(2.0) * a.dt);
-                            e = dp * dp * a.dt;
-                        } else {
-                            e = pn * pn * a.dt;
-                        }
-                        a.energy[i] = qtile(r, 5 + 2 * nrel)[qi] + e;
-                    }
-                    const long long ds = step - a.dft_start;
-                    if (a.n_dft > 0 && ds >= 0 && ds < a.dft_len && iz >= a.dz_lo && iz < a.dz_hi) {
-                        const long long pl = (long long)(iz - a.dz_lo) * a.plane + col;
+                    if (do_energy) a.energy[i] = energy_add(a, ent[k], pn, q1);
+                    if (do_dft && iz >= a.dz_lo && iz < a.dz_hi) {
+                        const long long pl = (long long)(iz - a.dz_lo) * a.plane + col[c];
                         const long long stride = (long long)(a.dz_hi - a.dz_lo) * a.plane;
                         const real* tw = a.tw + ds * a.n_dft * 2;
                         for (int j = 0; j < a.n_dft; ++j) {
-                            a.dre[j * stride + pl] += pn * tw[2 * j];
-                            a.dim[j * stride + pl] -= pn * tw[2 * j + 1];
+                            a.dre[j * stride + pl] = fma_(pn, tw[2 * j], a.dre[j * stride + pl]);
+                            a.dim[j * stride + pl] = fma_(-pn, tw[2 * j + 1], a.dim[j * stride + pl]);
                         }
                     }
                 }
@@ -265,7 +315,9 @@ __global__ void __launch_bounds__(TX* TY) wv_tma_kernel(const WvArgs<real> a, co
             issueQ(r + TMA_NQ);
         }
 #pragma unroll
-        for (int k = 0; k < 6; ++k) w[k] = w[k + 1];
+        for (int c = 0; c < CPT; ++c)
+#pragma unroll
+            for (int k = 0; k < 6; ++k) w[c][k] = w[c][k + 1];
     }
 }
 
