@@ -36,8 +36,8 @@ struct Variant { int tx, ty, zb, tma; };
 static const Variant kVariants[] = {
     {32, 8, 32, 0}, {32, 4, 32, 0}, {64, 4, 32, 0}, {32, 8, 64, 0},
     {32, 16, 16, 0}, {64, 8, 16, 0}, {128, 2, 32, 0}, {32, 8, 0, 0},
-    {32, 4, 32, 1}, {32, 8, 32, 1}, {64, 4, 32, 1}, {32, 4, 16, 1},
-    {32, 8, 16, 1}, {64, 4, 16, 1}, {32, 4, 64, 1}, {32, 8, 32, 1},
+    {32, 4, 32, 1}, {32, 8, 32, 1}, {32, 4, 24, 1}, {32, 4, 16, 1},
+    {32, 8, 16, 1}, {32, 4, 20, 1}, {32, 4, 40, 1}, {32, 8, 32, 1},
 };
 static const int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
@@ -263,9 +263,8 @@ static void launch_step(WvSession& S, int variant, int64_t s, int koff, cudaStre
         case 4: launch_step_t<real, 32, 16>(S, a, koff, st); break;
         case 5: launch_step_t<real, 64, 8>(S, a, koff, st); break;
         case 6: launch_step_t<real, 128, 2>(S, a, koff, st); break;
-        case 8: case 11: case 14: launch_tma_t<real, 32, 4, 1>(S, a, s, koff, st); break;
+        case 8: case 10: case 11: case 13: case 14: launch_tma_t<real, 32, 4, 1>(S, a, s, koff, st); break;
         case 9: case 12: launch_tma_t<real, 32, 8, 2>(S, a, s, koff, st); break;
-        case 10: case 13: launch_tma_t<real, 64, 4, 2>(S, a, s, koff, st); break;
         case 15: launch_tma_t<real, 32, 8, 1>(S, a, s, koff, st); break;
         default: fail(BD_ERR_INVALID_ARG, "bad tile variant %d", variant);
     }
