@@ -32,12 +32,12 @@ namespace bd {
 
 // Kernel variants: 0-7 plain (read-only-cache neighbours), 8-15 TMA-pipelined
 // (need a row pitch that is a multiple of 16 bytes).
-struct Variant { int tx, ty, zb, tma; };
+struct Variant { int tx, ty, zb, tma, cpt, zu; };
 static const Variant kVariants[] = {
-    {32, 8, 32, 0}, {32, 4, 32, 0}, {64, 4, 32, 0}, {32, 8, 64, 0},
-    {32, 16, 16, 0}, {64, 8, 16, 0}, {128, 2, 32, 0}, {32, 8, 0, 0},
-    {32, 4, 32, 1}, {32, 8, 32, 1}, {32, 4, 24, 1}, {32, 4, 16, 1},
-    {32, 8, 16, 1}, {32, 4, 20, 1}, {32, 4, 40, 1}, {32, 8, 32, 1},
+    {32, 8, 32, 0, 1, 1}, {32, 4, 32, 0, 1, 1}, {64, 4, 32, 0, 1, 1}, {32, 8, 64, 0, 1, 1},
+    {32, 16, 16, 0, 1, 1}, {64, 8, 16, 0, 1, 1}, {128, 2, 32, 0, 1, 1}, {32, 8, 0, 0, 1, 1},
+    {32, 4, 32, 1, 1, 1}, {32, 8, 32, 1, 2, 1}, {32, 4, 24, 1, 1, 2}, {32, 4, 16, 1, 1, 1},
+    {32, 8, 16, 1, 1, 2}, {32, 4, 20, 1, 1, 2}, {32, 4, 32, 1, 1, 2}, {32, 8, 32, 1, 1, 1},
 };
 static const int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
@@ -205,23 +205,23 @@ static void build_maps(WvSession& S, int tx, int ty) {
     S.maps_ty = ty;
 }
 
-template <class real, int TX, int TY, int CPT, int NREL>
+template <class real, int TX, int TY, int CPT, int NREL, int ZU>
 static void launch_tma_k(WvSession& S, const WvArgs<real>& a, const TmaMaps& maps, int koff, cudaStream_t st) {
     using L = TmaLayout<real, TX, TY, (NREL >= 0 ? NREL : BD_MAX_RELAX)>;
     static bool attr_done = false;
     if (!attr_done) {
-        BD_CUDA(cudaFuncSetAttribute(wv_tma_kernel<real, TX, TY, CPT, NREL>,
+        BD_CUDA(cudaFuncSetAttribute(wv_tma_kernel<real, TX, TY, CPT, NREL, ZU>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
         attr_done = true;
     }
     dim3 block(TX, TY / CPT, 1);
     dim3 grid((S.nx + TX - 1) / TX, (S.ny + TY - 1) / TY, (S.nz + a.zb - 1) / a.zb);
-    wv_tma_kernel<real, TX, TY, CPT, NREL><<<grid, block, L::SMEM, st>>>(a, S.kconst.as<WvConst<real>>(), koff, maps,
+    wv_tma_kernel<real, TX, TY, CPT, NREL, ZU><<<grid, block, L::SMEM, st>>>(a, S.kconst.as<WvConst<real>>(), koff, maps,
                                                                          S.flag.as<unsigned>() + 1);
     BD_LAUNCHED(S.ctx);
 }
 
-template <class real, int TX, int TY, int CPT>
+template <class real, int TX, int TY, int CPT, int ZU>
 static void launch_tma_t(WvSession& S, const WvArgs<real>& a, int64_t s, int koff, cudaStream_t st) {
     build_maps(S, TX, TY);
     TmaMaps maps;
@@ -236,10 +236,10 @@ static void launch_tma_t(WvSession& S, const WvArgs<real>& a, int64_t s, int kof
     if (S.has_cmap) maps.cmap = S.mC;
     // FP32 kernels with 0, 1 or 2 relaxation processes are compiled for their count;
     // FP64 and larger counts use the kernel that reads the count at run time
-    if (sizeof(real) == 4 && S.max_relax == 0) launch_tma_k<real, TX, TY, CPT, 0>(S, a, maps, koff, st);
-    else if (sizeof(real) == 4 && S.max_relax == 1) launch_tma_k<real, TX, TY, CPT, 1>(S, a, maps, koff, st);
-    else if (sizeof(real) == 4 && S.max_relax == 2) launch_tma_k<real, TX, TY, CPT, 2>(S, a, maps, koff, st);
-    else launch_tma_k<real, TX, TY, CPT, -1>(S, a, maps, koff, st);
+    if (sizeof(real) == 4 && S.max_relax == 0) launch_tma_k<real, TX, TY, CPT, 0, ZU>(S, a, maps, koff, st);
+    else if (sizeof(real) == 4 && S.max_relax == 1) launch_tma_k<real, TX, TY, CPT, 1, ZU>(S, a, maps, koff, st);
+    else if (sizeof(real) == 4 && S.max_relax == 2) launch_tma_k<real, TX, TY, CPT, 2, ZU>(S, a, maps, koff, st);
+    else launch_tma_k<real, TX, TY, CPT, -1, ZU>(S, a, maps, koff, st);
 }
 
 template <class real, int TX, int TY>
@@ -263,9 +263,11 @@ static void launch_step(WvSession& S, int variant, int64_t s, int koff, cudaStre
         case 4: launch_step_t<real, 32, 16>(S, a, koff, st); break;
         case 5: launch_step_t<real, 64, 8>(S, a, koff, st); break;
         case 6: launch_step_t<real, 128, 2>(S, a, koff, st); break;
-        case 8: case 10: case 11: case 13: case 14: launch_tma_t<real, 32, 4, 1>(S, a, s, koff, st); break;
-        case 9: case 12: launch_tma_t<real, 32, 8, 2>(S, a, s, koff, st); break;
-        case 15: launch_tma_t<real, 32, 8, 1>(S, a, s, koff, st); break;
+        case 8: case 11: launch_tma_t<real, 32, 4, 1, 1>(S, a, s, koff, st); break;
+        case 9: launch_tma_t<real, 32, 8, 2, 1>(S, a, s, koff, st); break;
+        case 10: case 13: case 14: launch_tma_t<real, 32, 4, 1, 2>(S, a, s, koff, st); break;
+        case 12: launch_tma_t<real, 32, 8, 1, 2>(S, a, s, koff, st); break;
+        case 15: launch_tma_t<real, 32, 8, 1, 1>(S, a, s, koff, st); break;
         default: fail(BD_ERR_INVALID_ARG, "bad tile variant %d", variant);
     }
     if (S.any_mur) {

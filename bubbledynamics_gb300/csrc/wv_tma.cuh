@@ -66,14 +66,23 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
     return ok != 0;
 }
 
-// Bounded wait: gives up after a fixed number of polls, records the timeout in
-// *err (bit 4) and returns false so the kernel can finish instead of hanging.
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Bounded wait: gives up after two seconds, records the timeout in *err
+// (bit 4) and returns false so the kernel can finish instead of hanging.
 // Once any wait has timed out, later waits return at once, so a broken
 // pipeline ends the kernel quickly.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, unsigned* err) {
-    for (int i = 0; i < (1 << 22); ++i) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const unsigned long long t0 = global_ns();
+    while (true) {
         if (mbar_try_wait(bar, parity)) return true;
-        if ((i & 1023) == 1023 && (*reinterpret_cast<volatile unsigned*>(err) & 4u)) return false;
+        if (*reinterpret_cast<volatile unsigned*>(err) & 4u) return false;
+        if (global_ns() - t0 > 2000000000ull) break;
     }
     atomicOr(err, 4u);
     return false;
@@ -105,9 +114,10 @@ struct TmaLayout {
 // One Westervelt step, TMA-pipelined.  Template parameters: tile TX x TY, CPT
 // cells per thread along y (the CTA has TX x TY/CPT threads), NREL relaxation
 // processes known at compile time (-1: read from the arguments, up to
-// BD_MAX_RELAX).  The cell update is cell_update(), so every variant gives the
+// BD_MAX_RELAX), ZU planes per loop iteration (one CTA barrier and one round
+// of TMA issues per ZU planes).  The cell update is cell_update(), so every variant gives the
 // same bits as the plain kernel.
-template <class real, int TX, int TY, int CPT, int NREL>
+template <class real, int TX, int TY, int CPT, int NREL, int ZU>
 __global__ void __launch_bounds__(TX* TY / CPT) wv_tma_kernel(const WvArgs<real> a,
                                                               const WvConst<real>* __restrict__ Kp, int koff,
                                                               const __grid_constant__ TmaMaps maps,
@@ -215,7 +225,11 @@ __global__ void __launch_bounds__(TX* TY / CPT) wv_tma_kernel(const WvArgs<real>
     const bool do_dft = a.n_dft > 0 && ds >= 0 && ds < a.dft_len;
     const bool single_mat = !a.matmap && !a.plane_mat;
 
-    for (int iz = z0; iz < z1; ++iz) {
+    for (int izg = z0; izg < z1; izg += ZU) {
+#pragma unroll
+    for (int u = 0; u < ZU; ++u) {
+        const int iz = izg + u;
+        if (iz >= z1) break;
         const int qc = iz - z0 + 3;                // stencil plane
         const int r = iz - z0;
         waitP(qc + 3);
@@ -309,15 +323,19 @@ __global__ void __launch_bounds__(TX* TY / CPT) wv_tma_kernel(const WvArgs<real>
                 }
             }
         }
-        __syncthreads();                           // everyone is done with plane iz and its tiles
-        if (tid == 0) {
-            issueP(qc + TMA_NP);
-            issueQ(r + TMA_NQ);
-        }
 #pragma unroll
         for (int c = 0; c < CPT; ++c)
 #pragma unroll
             for (int k = 0; k < 6; ++k) w[c][k] = w[c][k + 1];
+    }
+        __syncthreads();                           // everyone is done with planes izg..izg+ZU-1 and their tiles
+        if (tid == 0) {
+#pragma unroll
+            for (int u = 0; u < ZU; ++u) {
+                issueP(izg + u - z0 + 3 + TMA_NP);
+                issueQ(izg + u - z0 + TMA_NQ);
+            }
+        }
     }
 }
 
