@@ -132,7 +132,7 @@ class WesterveltOutputs(C.Structure):
 class FocalLoss(C.Structure):
     _fields_ = [
         ("focus_ix", i32), ("focus_iy", i32), ("focus_iz", i32),
-        ("focal_radius", i32), ("side_radius", i32), ("pad0", i32),
+        ("focal_radius", i32), ("side_radius", i32), ("checkpoint_every", i32),
         ("side_weight", f64),
         ("window_start", i64), ("window_end", i64),
     ]

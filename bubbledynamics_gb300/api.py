@@ -75,8 +75,7 @@ def load(path=None):
     _sig(L, "bd_gilmore_threshold", [P, P, P, C.c_int64, P, C.c_int64, C.c_int32, C.c_int64, P,
                                      C.POINTER(C.c_double)])
     _sig(L, "bd_heat_run_device_noalloc", [P, P, P, P, P, P, C.c_int64, P])
-    if hasattr(L, "bd_westervelt_adjoint"):
-        _sig(L, "bd_westervelt_adjoint", [P, P, P, P, P, P, C.POINTER(C.c_double), P, P, P])
+    _sig(L, "bd_westervelt_adjoint", [P, P, P, P, P, P, C.POINTER(C.c_double), P, P, P])
     _lib = L
     return L
 
@@ -194,6 +193,21 @@ class Context:
 
     def westervelt_session(self, prob: WesterveltProblem):
         return WesterveltSession(self, prob)
+
+    def westervelt_adjoint(self, prob: WesterveltProblem, loss):
+        """Loss of `loss` (abi.FocalLoss) and its gradient w.r.t. the element
+        phases and amplitudes of prob's BD_SRC_ARRAY source
+        (bd_westervelt_adjoint).  Returns (loss, grad_phase, grad_amp, timings)
+        with timings = {"forward_ms", "recompute_ms", "backward_ms"}."""
+        ne = prob.source.n_elements
+        gp = np.zeros(ne, np.float64)
+        ga = np.zeros(ne, np.float64)
+        tm = np.zeros(3, np.float64)
+        L = C.c_double(0.0)
+        check(self.L.bd_westervelt_adjoint(self.h, C.byref(prob.grid), C.byref(prob.medium), C.byref(prob.source),
+                                           C.byref(prob.params), C.byref(loss), C.byref(L), _ptr(gp), _ptr(ga),
+                                           _ptr(tm)))
+        return L.value, gp, ga, {"forward_ms": tm[0], "recompute_ms": tm[1], "backward_ms": tm[2]}
 
     # ------------------------------------------------------------ heat
     def heat(self, thermal, Q, traj, max_steps=0, snapshot_legs=(), want_T=True, want_dose=True):

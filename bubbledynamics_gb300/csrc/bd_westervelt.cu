@@ -27,6 +27,7 @@
 #include "bd_internal.h"
 #include "wv_kernels.cuh"
 #include "wv_tma.cuh"
+#include "wv_adjoint.cuh"
 
 namespace bd {
 
@@ -801,6 +802,194 @@ static void ck_load(WvSession& S, const void* blob, size_t bytes) {
     S.step = h.step;
 }
 
+
+// ---------------------------------------------------------------- adjoint
+template <class real>
+static void adj_launch(WvSession& S, const AdjArgs<real>& a, cudaStream_t st) {
+    const WvConst<real>* K = S.kconst.as<WvConst<real>>();
+    dim3 b(32, 8), g((S.nx + 31) / 32, (S.ny + 7) / 8, S.nz);
+    switch (S.max_relax) {
+        case 0: adj_pass1_kernel<real, 0><<<g, b, 0, st>>>(a, K); break;
+        case 1: adj_pass1_kernel<real, 1><<<g, b, 0, st>>>(a, K); break;
+        case 2: adj_pass1_kernel<real, 2><<<g, b, 0, st>>>(a, K); break;
+        default: adj_pass1_kernel<real, BD_MAX_RELAX><<<g, b, 0, st>>>(a, K); break;
+    }
+    BD_LAUNCHED(S.ctx);
+    switch (S.max_relax) {
+        case 0: adj_pass2_kernel<real, 0><<<g, b, 0, st>>>(a, K); break;
+        case 1: adj_pass2_kernel<real, 1><<<g, b, 0, st>>>(a, K); break;
+        case 2: adj_pass2_kernel<real, 2><<<g, b, 0, st>>>(a, K); break;
+        default: adj_pass2_kernel<real, BD_MAX_RELAX><<<g, b, 0, st>>>(a, K); break;
+    }
+    BD_LAUNCHED(S.ctx);
+}
+
+template <class real>
+static void adjoint_solve(WvSession& S, const bd_focal_loss* loss, double* loss_out, double* grad_phase,
+                          double* grad_amp, double* timings) {
+    cudaStream_t st = S.ctx->stream;
+    const int64_t N = S.p.n_steps;
+    const int64_t Kc = loss->checkpoint_every > 0 ? loss->checkpoint_every
+                                                  : std::max<int64_t>(1, (int64_t)std::ceil(std::sqrt((double)N)));
+    const int64_t nck = (N + Kc - 1) / Kc;
+    const size_t f = S.ncell * S.esz;
+    const int nlev = 5 + 2 * S.max_relax;
+    // forward with checkpoints at steps 0, Kc, 2Kc, ...
+    std::vector<PoolBuf> ck(std::max<int64_t>(nck, 1) * nlev);
+    for (auto& b : ck) b.alloc(S.ctx, f);
+    auto level_buf = [&](int64_t s, int k) -> PoolBuf& {   // k < 5: p^{s-k}; 5 + 2v + j: R^{s-1-j} of process v
+        if (k < 5) return S.P[(head_of(s) + k) % 5];
+        const int v = (k - 5) / 2, j = (k - 5) % 2;
+        return S.R[v][(int)(s & 1) ^ j];
+    };
+    BD_CUDA(cudaEventRecord(S.ctx->ev0, st));
+    for (int64_t c = 0; c < nck; ++c) {
+        const int64_t s0 = c * Kc;
+        for (int k = 0; k < nlev; ++k)
+            BD_CUDA(cudaMemcpyAsync(ck[c * nlev + k].p, level_buf(s0, k).p, f, cudaMemcpyDeviceToDevice, st));
+        advance(S, std::min<int64_t>(Kc, N - s0), S.p.graph_chunk >= 0);
+    }
+    BD_CUDA(cudaEventRecord(S.ctx->ev1, st));
+    BD_CUDA(cudaEventSynchronize(S.ctx->ev1));
+    float ms_fwd = 0;
+    BD_CUDA(cudaEventElapsedTime(&ms_fwd, S.ctx->ev0, S.ctx->ev1));
+    // loss = sum_x w_L(x) E(x)
+    std::vector<real> E(S.ncell);
+    BD_CUDA(cudaMemcpy(E.data(), S.energy.p, f, cudaMemcpyDeviceToHost));
+    const int fr2 = loss->focal_radius * loss->focal_radius, sr2 = loss->side_radius * loss->side_radius;
+    double L = 0.0;
+    for (int iz = 0; iz < S.nz; ++iz)
+        for (int iy = 0; iy < S.ny; ++iy)
+            for (int ix = 0; ix < S.nx; ++ix) {
+                const int dx = ix - loss->focus_ix, dy = iy - loss->focus_iy, dz = iz - loss->focus_iz;
+                const int r2 = dx * dx + dy * dy + dz * dz;
+                double wl = 0.0;
+                if (r2 <= fr2) wl = -1.0;
+                else if (iz == loss->focus_iz && r2 >= sr2) wl = loss->side_weight;
+                if (wl != 0.0) L += wl * (double)E[((size_t)iz * S.ny + iy) * S.nx + ix];
+            }
+    if (loss_out) *loss_out = L;
+    // backward buffers
+    PoolBuf mu[5], muR[BD_MAX_RELAX][2], H, gphi, gamp, eamp;
+    for (auto& b : mu) { b.alloc(S.ctx, f); BD_CUDA(cudaMemsetAsync(b.p, 0, f, st)); }
+    for (int v = 0; v < S.max_relax; ++v)
+        for (auto& b : muR[v]) { b.alloc(S.ctx, f); BD_CUDA(cudaMemsetAsync(b.p, 0, f, st)); }
+    H.alloc(S.ctx, f);
+    gphi.alloc(S.ctx, S.plane * 8); gamp.alloc(S.ctx, S.plane * 8);
+    BD_CUDA(cudaMemsetAsync(gphi.p, 0, S.plane * 8, st));
+    BD_CUDA(cudaMemsetAsync(gamp.p, 0, S.plane * 8, st));
+    std::vector<double> ea(S.plane, 0.0);
+    std::vector<int> elem(S.plane, -1);
+    for (long long j = 0; j < S.plane; ++j) {
+        if (S.s.kind == BD_SRC_ARRAY) {
+            const int e = S.s.element_of_cell[j];
+            if (e >= 0 && e < S.s.n_elements) { elem[j] = e; ea[j] = S.s.element_amp ? S.s.element_amp[e] : 1.0; }
+        } else {
+            ea[j] = 1.0;
+        }
+    }
+    upload(S, eamp, ea);
+    std::vector<PoolBuf> seg(Kc + 5);
+    for (auto& b : seg) b.alloc(S.ctx, f);
+    // recompute without accumulators
+    const bd_westervelt_params saved = S.p;
+    S.p.peak_end = S.p.peak_start;
+    S.p.energy_end = S.p.energy_start;
+    S.p.dft_len = 0;
+    const int n_dft_saved = S.n_dft;
+    S.n_dft = 0;
+    AdjArgs<real> a;
+    std::memset(&a, 0, sizeof a);
+    a.nx = S.nx; a.ny = S.ny; a.nz = S.nz; a.plane = S.plane;
+    a.max_relax = S.max_relax;
+    a.cmap = S.has_cmap ? S.cmap.as<float>() : nullptr;
+    a.matmap = S.has_matmap ? S.matmap.as<uint8_t>() : nullptr;
+    a.plane_mat = S.has_planemat ? S.planemat.as<int>() : nullptr;
+    if (S.g.sponge_cells > 0) { a.wx = S.wx.as<real>(); a.wy = S.wy.as<real>(); a.wz = S.wz.as<real>(); }
+    a.kxy180 = (real)(S.g.dt * S.g.dt / (S.g.dx * S.g.dx) / 180.0);
+    a.kz180 = (real)(S.g.dt * S.g.dt / (S.g.dz * S.g.dz) / 180.0);
+    a.dt2 = (real)(S.g.dt * S.g.dt);
+    a.dt = (real)S.g.dt;
+    a.relax_scheme = S.p.relax_scheme;
+    a.src_iz = (S.s.kind != BD_SRC_NONE) ? S.s.plane_iz : -1;
+    a.H = H.as<real>();
+    a.gphi = gphi.as<double>(); a.gamp = gamp.as<double>(); a.e_amp = eamp.as<double>();
+    a.sAf = S.sAf.as<float>(); a.sPsi = S.sPsi.as<float>(); a.sTauf = S.sTauf.as<float>();
+    a.theta = S.theta.as<float>(); a.tb0 = S.tb0.as<float>();
+    a.sA = S.sA.as<double>(); a.sVar = S.sVar.as<double>(); a.sTau = S.sTau.as<double>(); a.sPhi = S.sPhi.as<double>();
+    a.t_src = S.t_src.as<double>();
+    a.n_tones = S.s.n_tones;
+    a.burst = S.s.burst_cycles > 0.0;
+    for (int k = 0; k < BD_MAX_TONES; ++k) {
+        a.freq[k] = S.s.freq[k]; a.tamp[k] = S.s.amp[k]; a.tphase[k] = S.s.phase[k]; a.tampf[k] = (float)S.s.amp[k];
+    }
+    a.tau_max = S.tau_max;
+    a.burst_len = a.burst ? S.s.burst_cycles / S.s.freq[0] : 0.0;
+    a.burst_lenf = (float)a.burst_len;
+    a.fx = loss->focus_ix; a.fy = loss->focus_iy; a.fz = loss->focus_iz;
+    a.frad2 = fr2; a.srad2 = sr2; a.side_w = loss->side_weight;
+    int rot = 0, rrot = 0;    // rotation of the adjoint rings
+    float ms_rec = 0, ms_bwd = 0;
+    for (int64_t c = nck - 1; c >= 0; --c) {
+        const int64_t s0 = c * Kc, s1 = std::min<int64_t>(N, s0 + Kc);
+        BD_CUDA(cudaEventRecord(S.ctx->ev0, st));
+        for (int k = 0; k < nlev; ++k)
+            BD_CUDA(cudaMemcpyAsync(level_buf(s0, k).p, ck[c * nlev + k].p, f, cudaMemcpyDeviceToDevice, st));
+        long long sb = s0;
+        BD_CUDA(cudaMemcpyAsync(S.step_base.p, &sb, sizeof sb, cudaMemcpyHostToDevice, st));
+        BD_CUDA(cudaStreamSynchronize(st));
+        S.step = s0;
+        // seg[j] holds p^{s0 - 4 + j}
+        for (int k = 0; k < 5; ++k)
+            BD_CUDA(cudaMemcpyAsync(seg[4 - k].p, ck[c * nlev + k].p, f, cudaMemcpyDeviceToDevice, st));
+        for (int64_t s = s0; s < s1; ++s) {
+            issue_steps(S, S.variant, s, 1, st);
+            S.step = s + 1;
+            BD_CUDA(cudaMemcpyAsync(seg[s - s0 + 5].p, S.P[head_of(s + 1)].p, f, cudaMemcpyDeviceToDevice, st));
+        }
+        BD_CUDA(cudaEventRecord(S.ctx->ev1, st));
+        for (int64_t s = s1 - 1; s >= s0; --s) {
+            for (int k = 0; k < 5; ++k) a.mu[k] = mu[(rot + k) % 5].as<real>();
+            for (int v = 0; v < S.max_relax; ++v) {
+                a.muR1[v] = muR[v][rrot].as<real>();
+                a.muR2[v] = muR[v][rrot ^ 1].as<real>();
+            }
+            for (int k = 0; k < 5; ++k) a.fp[k] = seg[s - s0 + 5 - k].as<real>();
+            a.step = s;
+            a.in_window = (s >= loss->window_start && s < loss->window_end) ? 1 : 0;
+            adj_launch<real>(S, a, st);
+            rot = (rot + 1) % 5;      // lambda_k now sits in the buffer of mu_{k+1}
+            rrot ^= 1;
+        }
+        cudaEvent_t e2;
+        BD_CUDA(cudaEventCreate(&e2));
+        BD_CUDA(cudaEventRecord(e2, st));
+        BD_CUDA(cudaEventSynchronize(e2));
+        float m1 = 0, m2 = 0;
+        BD_CUDA(cudaEventElapsedTime(&m1, S.ctx->ev0, S.ctx->ev1));
+        BD_CUDA(cudaEventElapsedTime(&m2, S.ctx->ev1, e2));
+        cudaEventDestroy(e2);
+        ms_rec += m1;
+        ms_bwd += m2;
+    }
+    S.p = saved;
+    S.n_dft = n_dft_saved;
+    // per-element sums of the per-cell gradients
+    std::vector<double> gp(S.plane), ga(S.plane);
+    BD_CUDA(cudaMemcpy(gp.data(), gphi.p, S.plane * 8, cudaMemcpyDeviceToHost));
+    BD_CUDA(cudaMemcpy(ga.data(), gamp.p, S.plane * 8, cudaMemcpyDeviceToHost));
+    const int ne = S.s.kind == BD_SRC_ARRAY ? S.s.n_elements : 0;
+    if (grad_phase) for (int e = 0; e < ne; ++e) grad_phase[e] = 0.0;
+    if (grad_amp) for (int e = 0; e < ne; ++e) grad_amp[e] = 0.0;
+    for (long long j = 0; j < S.plane; ++j) {
+        const int e = elem[j];
+        if (e < 0) continue;
+        if (grad_phase) grad_phase[e] += gp[j];
+        if (grad_amp) grad_amp[e] += ga[j];
+    }
+    if (timings) { timings[0] = ms_fwd; timings[1] = ms_rec; timings[2] = ms_bwd; }
+}
+
 }  // namespace bd
 
 struct bd_westervelt {
@@ -907,6 +1096,32 @@ bd_status bd_checkpoint_load(bd_westervelt* w, const void* blob, size_t bytes) {
         if (!w || !blob) fail(BD_ERR_INVALID_ARG, "null argument");
         ctx_check(w->S.ctx);
         ck_load(w->S, blob, bytes);
+    });
+}
+
+bd_status bd_westervelt_adjoint(bd_context* ctx, const bd_grid* grid, const bd_medium* medium, const bd_source* source,
+                                const bd_westervelt_params* params, const bd_focal_loss* loss, double* loss_out,
+                                double* grad_phase, double* grad_amp, double* timings_ms) {
+    return guard([&] {
+        ctx_check(ctx);
+        if (!grid || !loss || !params) fail(BD_ERR_INVALID_ARG, "null argument");
+        for (int f = 0; f < 6; ++f)
+            if (grid->face[f] != BD_FACE_OPEN) fail(BD_ERR_UNSUPPORTED, "the adjoint supports OPEN faces only");
+        if (!source || source->kind == BD_SRC_NONE) fail(BD_ERR_INVALID_ARG, "the adjoint needs a source");
+        if (loss->window_start < 0 || loss->window_end > params->n_steps || loss->window_start >= loss->window_end)
+            fail(BD_ERR_INVALID_ARG, "bad loss window");
+        bd_westervelt_params p = *params;
+        p.energy_mode = BD_ENERGY_P2;
+        p.energy_start = loss->window_start;
+        p.energy_end = loss->window_end;
+        p.peak_start = p.peak_end = 0;
+        p.n_dft = 0;
+        p.q_mode = BD_Q_NONE;
+        p.fault_at_step = -1;
+        bd_westervelt w;
+        setup(w.S, ctx, grid, medium, source, &p);
+        if (w.S.prec == BD_F32) adjoint_solve<float>(w.S, loss, loss_out, grad_phase, grad_amp, timings_ms);
+        else adjoint_solve<double>(w.S, loss, loss_out, grad_phase, grad_amp, timings_ms);
     });
 }
 

@@ -371,6 +371,128 @@ def cfg1(nx=128, ny=128, nz=256, n_steps=3000, precision=abi.BD_F32, seed=1, het
 
 
 # --------------------------------------------------------------------------
+# phased-array focusing problem of the adjoint (3 z-slabs, cap-shaped array)
+# --------------------------------------------------------------------------
+def fibonacci_cap(n, alpha):
+    """n points spread evenly over the spherical cap of half-angle alpha
+    (Fibonacci lattice): polar angles theta_k and azimuths phi_k."""
+    k = np.arange(n, dtype=np.float64) + 0.5
+    cos_t = 1.0 - (1.0 - math.cos(alpha)) * k / n
+    theta = np.arccos(cos_t)
+    phi = np.mod(k * math.pi * (3.0 - math.sqrt(5.0)), 2.0 * math.pi)
+    return theta, phi
+
+
+def slab_materials(f):
+    """Water / fat / liver (c, rho, beta, delta, relaxation)."""
+    water = _material(1500.0, 1000.0, 3.5, water_delta(f, 1500.0))
+    fat = _material(1450.0, 950.0, 6.0, 4.0 * water_delta(f, 1450.0), relax=((3.0, 2.0e-7),))
+    liver = _material(1590.0, 1060.0, 4.25, 3.0 * water_delta(f, 1590.0), relax=((5.0, 1.0e-7),))
+    return [water, fat, liver]
+
+
+def focal_array_problem(nx, ny, nz, dx, n_elements, n_steps, window, F, aperture, precision=abi.BD_F32,
+                        seed=4, f=1.0e6, p0=0.3e6, sponge=None, slabs=(0.35, 0.55), jitter_cells=1.5,
+                        focal_radius=2, side_radius=None, side_weight=0.1, name="focal_array"):
+    """A cap-shaped phased array focusing through water / fat / liver slabs.
+
+    The source plane (iz = sponge) carries the bowl delay law of focal length F
+    and planar aperture radius `aperture`; element k covers the plane cells
+    nearest to the projection F tan(theta_k) (cos phi_k, sin phi_k) of its
+    Fibonacci cap point.  Initial element phases are U[0, 2 pi) from `seed`,
+    amplitudes 1.  Slab interfaces sit at the fractions `slabs` of the depth
+    between the source plane and the far sponge, each displaced per (x, y) by a
+    seeded Gaussian-correlated jitter of up to `jitter_cells`.  Continuous wave
+    at f; the loss window is the last part of the run.  Returns (problem, loss)."""
+    sponge = sponge if sponge is not None else max(4, min(nx, ny, nz) // 10)
+    c_max = 1590.0
+    dt = 0.3 * dx / c_max
+    g = abi.Grid()
+    g.nx, g.ny, g.nz = nx, ny, nz
+    g.x0 = -0.5 * (nx - 1) * dx
+    g.y0 = -0.5 * (ny - 1) * dx
+    g.z0 = -sponge * dx
+    g.dx = g.dz = dx
+    g.dt = dt
+    g.face[:] = [abi.BD_FACE_OPEN] * 6
+    g.mur_layers = 0
+    g.sponge_cells = sponge
+    g.sponge_strength = 0.35
+    med = abi.Medium()
+    mats = slab_materials(f)
+    med.n_materials = len(mats)
+    for k, m in enumerate(mats):
+        med.mat[k] = m
+    src = abi.Source()
+    src.kind = abi.BD_SRC_ARRAY
+    src.plane_iz = sponge
+    src.focal_length = F
+    src.alpha = math.atan(aperture / F)
+    src.alpha_hole = 0.0
+    src.p0 = p0
+    src.c_delay = 1500.0
+    src.n_tones = 1
+    src.freq[0] = f
+    src.amp[0] = 1.0
+    src.burst_cycles = 0.0
+    p = _params_default(n_steps, precision)
+    p.relax_scheme = abi.BD_RELAX_SEMI_IMPLICIT
+    p.peak_start = p.peak_end = 0
+    p.energy_start, p.energy_end = window
+    prob = WesterveltProblem(name, g, med, src, p, meta={"f": f})
+    rng = np.random.default_rng(seed)
+    # slabs with jittered interfaces
+    depth = nz - 2 * sponge
+    z = np.arange(nz).reshape(nz, 1, 1)
+    mm = np.zeros((nz, ny, nx), np.uint8)
+    for k, frac in enumerate(slabs):
+        jit = gaussian_heterogeneity((ny, nx), max(1.0, 1.0e-3 / dx), seed + 10 + k) * jitter_cells
+        zi = sponge + frac * depth + jit.reshape(1, ny, nx)
+        mm[z >= zi] = k + 1
+    prob.set_material_map(mm)
+    # elements: nearest projected cap point for every plane cell inside the aperture
+    theta, phi = fibonacci_cap(n_elements, math.atan(aperture / F))
+    ex = F * np.tan(theta) * np.cos(phi)
+    ey = F * np.tan(theta) * np.sin(phi)
+    xs = g.x0 + dx * np.arange(nx)
+    ys = g.y0 + dx * np.arange(ny)
+    X, Y = np.meshgrid(xs, ys, indexing="xy")
+    d2 = (X[..., None] - ex) ** 2 + (Y[..., None] - ey) ** 2
+    elem = np.argmin(d2, axis=-1).astype(np.int32)
+    elem[np.hypot(X, Y) > aperture] = -1
+    phase = rng.uniform(0.0, 2.0 * math.pi, n_elements)
+    prob.set_elements(elem.reshape(-1), phase, np.ones(n_elements))
+    loss = abi.FocalLoss()
+    loss.focus_ix, loss.focus_iy = nx // 2, ny // 2
+    loss.focus_iz = min(nz - sponge - 1, sponge + int(round(F / dx)))
+    loss.focal_radius = focal_radius
+    loss.side_radius = side_radius if side_radius is not None else 3 * focal_radius
+    loss.checkpoint_every = 0
+    loss.side_weight = side_weight
+    loss.window_start, loss.window_end = window
+    return prob, loss
+
+
+def cfg4(n_steps=4000, precision=abi.BD_F32, seed=4):
+    """Adjoint configuration: 192^3 at dx = 0.2 mm, water / fat / liver slabs
+    with jittered interfaces, 256-element cap array (F = 25 mm, aperture
+    radius 14 mm) at 1 MHz CW with seeded random phases, 20-cell sponge;
+    loss = -(focal energy) + 0.1 (focal-plane side-lobe energy) over the
+    last quarter of the run."""
+    w = (3 * n_steps // 4, n_steps)
+    return focal_array_problem(192, 192, 192, 0.2e-3, 256, n_steps, w, 25e-3, 14e-3, precision=precision,
+                               seed=seed, sponge=20, focal_radius=4, side_radius=12, name="cfg4")
+
+
+def adjoint_mini(precision=abi.BD_F64, n_elements=16, n_steps=200, seed=4):
+    """The cfg4 physics on a 24 x 24 x 36 box (dx = 0.2 mm, 16 elements) for
+    gradient checks."""
+    w = (n_steps - 60, n_steps)
+    return focal_array_problem(24, 24, 36, 0.2e-3, n_elements, n_steps, w, 3.6e-3, 1.5e-3, precision=precision,
+                               seed=seed, sponge=4, focal_radius=2, side_radius=5, name="adjoint_mini")
+
+
+# --------------------------------------------------------------------------
 # bioheat program (T:114-224)
 # --------------------------------------------------------------------------
 class ThermalProblem:

@@ -234,14 +234,17 @@ typedef struct bd_focal_loss {
     int32_t focus_ix, focus_iy, focus_iz;
     int32_t focal_radius;
     int32_t side_radius;
-    int32_t pad0;
+    int32_t checkpoint_every;           /* forward checkpoint interval (0 = ceil(sqrt(n_steps))) */
     double side_weight;
     int64_t window_start, window_end;   /* step window [start, end) */
 } bd_focal_loss;
 
 /* Gradient of the loss with respect to element phases and amplitudes of a
  * BD_SRC_ARRAY source (no counterpart in the reference; the forward model is
- * W:139-236 + W:62-85).  Uses sqrt(N) checkpointing; FP32 fields. */
+ * W:139-236 + W:62-85).  Discrete adjoint of the step, sqrt(N) forward
+ * checkpoints with recomputation per segment; OPEN faces only.  grad_phase /
+ * grad_amp have n_elements entries; timings_ms (may be NULL) receives the
+ * forward, recompute and backward device times. */
 bd_status bd_westervelt_adjoint(bd_context* ctx, const bd_grid* grid, const bd_medium* medium,
                                 const bd_source* source, const bd_westervelt_params* params,
                                 const bd_focal_loss* loss, double* loss_out,

@@ -402,6 +402,182 @@ bd_status wv_run(const bd_grid* g, const bd_medium* m, const bd_source* s,
     return BD_OK;
 }
 
+/* Discrete adjoint of wv_run<double> for OPEN faces (no reference
+ * counterpart; the forward model is W:139-236 with the source of W:62-85).
+ * Written in scatter form: every forward operation, visited in reverse,
+ * pushes its output adjoint onto its inputs.  All forward time levels are
+ * kept (small grids only), so no checkpointing is involved.  Loss:
+ * L = sum_x w(x) E(x), E the p^2 dt energy over the loss window, w = -1 in the
+ * focal ball, side_weight on the focal plane outside side_radius. */
+bd_status wv_adjoint(const bd_grid* g, const bd_medium* m, const bd_source* s, const bd_westervelt_params* p0,
+                     const bd_focal_loss* loss, double* loss_out, double* grad_phase, double* grad_amp) {
+    for (int f = 0; f < 6; ++f)
+        if (g->face[f] != BD_FACE_OPEN) return BD_ERR_UNSUPPORTED;
+    if (!s || s->kind != BD_SRC_ARRAY) return BD_ERR_INVALID_ARG;
+    bd_westervelt_params p = *p0;
+    p.energy_mode = BD_ENERGY_P2;
+    p.energy_start = loss->window_start;
+    p.energy_end = loss->window_end;
+    p.peak_start = p.peak_end = 0;
+    p.n_dft = 0;
+    WvRun<double> W;
+    W.g = g; W.m = m; W.s = s; W.p = &p;
+    if (!wv_setup(g, m, s, W.S)) return BD_ERR_INVALID_ARG;
+    W.init();
+    const WvSetup& S = W.S;
+    const int nx = S.nx, ny = S.ny, nz = S.nz;
+    const size_t n = S.ncell;
+    const int64_t N = p.n_steps;
+    const double dt = g->dt;
+    std::vector<std::vector<double>> hist(N + 1);   /* hist[t] = p^t */
+    std::vector<double> tsrc(N);
+    hist[0].assign(n, 0.0);
+    for (int64_t st = 0; st < N; ++st) {
+        tsrc[st] = p.t_src ? p.t_src[st] : p.t0 + (double)(st + 1) * dt;
+        W.step(st, tsrc[st]);
+        hist[st + 1] = W.P[W.head];
+    }
+    auto wloss = [&](int ix, int iy, int iz) {
+        const int dx = ix - loss->focus_ix, dy = iy - loss->focus_iy, dz = iz - loss->focus_iz;
+        const int r2 = dx * dx + dy * dy + dz * dz;
+        if (r2 <= loss->focal_radius * loss->focal_radius) return -1.0;
+        if (iz == loss->focus_iz && r2 >= loss->side_radius * loss->side_radius) return loss->side_weight;
+        return 0.0;
+    };
+    double L = 0.0;
+    for (int iz = 0; iz < nz; ++iz)
+        for (int iy = 0; iy < ny; ++iy)
+            for (int ix = 0; ix < nx; ++ix) L += wloss(ix, iy, iz) * W.energy[cidx(ix, iy, iz, nx, ny)];
+    if (loss_out) *loss_out = L;
+    /* adjoints of every level: ap[t] for p^t (t = 0..N), ar[v][t + 2] for R^t (t = -2..N-1) */
+    std::vector<std::vector<double>> ap(N + 1, std::vector<double>(n, 0.0));
+    const int NR = S.max_relax;
+    std::vector<std::vector<double>> ar[BD_MAX_RELAX];
+    for (int v = 0; v < NR; ++v) ar[v].assign(N + 2, std::vector<double>(n, 0.0));
+    const size_t np = (size_t)nx * ny;
+    std::vector<double> gphi(np, 0.0), gamp(np, 0.0);
+    const double coef[4] = {-490.0, 270.0, -27.0, 2.0};
+    auto lev = [&](int64_t t, size_t i) { return t >= 0 ? hist[t][i] : 0.0; };
+    for (int64_t st = N - 1; st >= 0; --st) {
+        std::vector<double>& A = ap[st + 1];          /* complete: later steps were visited first */
+        if (st >= loss->window_start && st < loss->window_end)
+            for (int iz = 0; iz < nz; ++iz)
+                for (int iy = 0; iy < ny; ++iy)
+                    for (int ix = 0; ix < nx; ++ix) {
+                        const size_t i = cidx(ix, iy, iz, nx, ny);
+                        A[i] += 2.0 * wloss(ix, iy, iz) * hist[st + 1][i] * dt;
+                    }
+        auto push = [&](int64_t t, size_t i, double v) { if (t >= 0) ap[t][i] += v; };
+        for (int iz = 0; iz < nz; ++iz)
+            for (int iy = 0; iy < ny; ++iy)
+                for (int ix = 0; ix < nx; ++ix) {
+                    const size_t i = cidx(ix, iy, iz, nx, ny);
+                    const double gout = A[i];
+                    if (iz == S.src_iz) {
+                        /* S_j(t) = A_j sum_k a_k sin(2 pi f_k tt + phi_k + phi_e) / var_j */
+                        const size_t j = (size_t)iy * nx + ix;
+                        if (!S.srcOn[j]) continue;
+                        double tt = tsrc[st] + S.srcTau[j];
+                        if (s->burst_cycles > 0.0) {
+                            const double tb = tt - S.tau_max;
+                            if (tb < 0.0 || tb >= s->burst_cycles / s->freq[0]) continue;
+                            tt = tb;
+                        }
+                        double sn = 0.0, cs = 0.0;
+                        for (int k = 0; k < s->n_tones; ++k) {
+                            const double ang = 2 * M_PI * s->freq[k] * tt + s->phase[k] + S.srcPhi[j];
+                            sn += s->amp[k] * std::sin(ang);
+                            cs += s->amp[k] * std::cos(ang);
+                        }
+                        gphi[j] += gout * S.srcA[j] * cs / S.srcVar[j];
+                        const int e = s->element_of_cell[j];
+                        const double ae = s->element_amp ? s->element_amp[e] : 1.0;
+                        if (ae != 0.0) gamp[j] += gout * S.srcA[j] * sn / S.srcVar[j] / ae;
+                        continue;
+                    }
+                    const bd_material& mt = m->mat[S.mat[i]];
+                    const double c = S.c[i];
+                    const double w = S.wx[ix] * S.wy[iy] * S.wz[iz];
+                    const double gpn = gout * w;                  /* p^{s+1} = w pn */
+                    const double kxy = std::pow(c * dt / g->dx, 2) / 180.0, kz = std::pow(c * dt / g->dz, 2) / 180.0;
+                    const double kd = mt.delta / (2.0 * dt * c * c), kn = 2.0 * mt.beta / (mt.rho * c * c);
+                    const double kr = std::pow(c * dt, 2);
+                    const double P0 = lev(st, i), P1 = lev(st - 1, i), P2 = lev(st - 2, i), P3 = lev(st - 3, i);
+                    double gY = 0.0, gDttt = 0.0, gE = 0.0;
+                    if (mt.n_relax > 0 && p.relax_scheme == BD_RELAX_SEMI_IMPLICIT) {
+                        double av[BD_MAX_RELAX], bc[BD_MAX_RELAX], sa = 0.0, g_pn = gpn;
+                        for (int v = 0; v < mt.n_relax; ++v) {
+                            const double tau = mt.relax_tau[v], cv = mt.relax_c[v];
+                            av[v] = (2.0 * dt * 2.0 * cv * tau) / (2.0 * dt * dt * dt) / ((2.0 * dt + 3.0 * tau) * c * c * c);
+                            bc[v] = tau / (2.0 * dt + 3.0 * tau);
+                            sa += av[v];
+                            g_pn += 3.0 * av[v] * ar[v][st + 2][i];       /* R^s = a (3 pn + E) + b B */
+                        }
+                        const double den = 1.0 - 3.0 * kr * sa;      /* pn = (Y + kr G) / den */
+                        gY = g_pn / den;
+                        const double gG = g_pn * kr / den;
+                        for (int v = 0; v < mt.n_relax; ++v) {
+                            const double gR = ar[v][st + 2][i];
+                            gE += av[v] * (gG + gR);
+                            const double gB = bc[v] * (gG + gR);      /* B = 4 R^{s-1} - R^{s-2} */
+                            ar[v][st + 1][i] += 4.0 * gB;
+                            ar[v][st][i] -= gB;
+                        }
+                        gDttt = kd * gY;
+                    } else {
+                        gY = gpn;
+                        gDttt = kd * gpn;
+                        for (int v = 0; v < mt.n_relax; ++v) {
+                            const double tau = mt.relax_tau[v], cv = mt.relax_c[v];
+                            const double ra = (2.0 * dt * 2.0 * cv * tau) / (2.0 * dt * dt * dt) / ((2.0 * dt + 3.0 * tau) * c * c * c);
+                            const double rb = tau / (2.0 * dt + 3.0 * tau);
+                            const double gR = ar[v][st + 2][i] + kr * gpn;   /* pn = Y + kr sum R */
+                            gDttt += ra * gR;
+                            ar[v][st + 1][i] += 4.0 * rb * gR;
+                            ar[v][st][i] -= rb * gR;
+                        }
+                    }
+                    /* Y = 2 P0 - P1 + Lap(P0) + kd Dttt + kn (D1 + D2) */
+                    push(st, i, 2.0 * gY);
+                    push(st - 1, i, -gY);
+                    for (int o = -3; o <= 3; ++o) {
+                        const double cf = coef[o < 0 ? -o : o];
+                        auto nb = [&](int jx, int jy, int jz, double k) {
+                            if (jx < 0 || jy < 0 || jz < 0 || jx >= nx || jy >= ny || jz >= nz) return;
+                            push(st, cidx(jx, jy, jz, nx, ny), k * cf * gY);
+                        };
+                        nb(ix + o, iy, iz, kxy);
+                        nb(ix, iy + o, iz, kxy);
+                        nb(ix, iy, iz + o, kz);
+                    }
+                    const double s3 = 3.0 * P0 - 4.0 * P1 + P2;
+                    const double gN = kn * gY;                   /* D1 = s3^2 / 4, D2 = P0 (2P0 - 5P1 + 4P2 - P3) */
+                    push(st, i, gN * (0.5 * s3 * 3.0 + (2.0 * P0 - 5.0 * P1 + 4.0 * P2 - P3) + 2.0 * P0));
+                    push(st - 1, i, gN * (0.5 * s3 * -4.0 - 5.0 * P0));
+                    push(st - 2, i, gN * (0.5 * s3 + 4.0 * P0));
+                    push(st - 3, i, gN * -P0);
+                    /* Dttt = 5 P0 - 18 P1 + 24 P2 - 14 P3 + 3 P4; E = -10 P0 + 12 P1 - 6 P2 + P3 */
+                    push(st, i, 5.0 * gDttt - 10.0 * gE);
+                    push(st - 1, i, -18.0 * gDttt + 12.0 * gE);
+                    push(st - 2, i, 24.0 * gDttt - 6.0 * gE);
+                    push(st - 3, i, -14.0 * gDttt + gE);
+                    push(st - 4, i, 3.0 * gDttt);
+                }
+    }
+    const int ne = s->n_elements;
+    for (int e = 0; e < ne; ++e) {
+        if (grad_phase) grad_phase[e] = 0.0;
+        if (grad_amp) grad_amp[e] = 0.0;
+    }
+    for (size_t j = 0; j < np; ++j) {
+        if (!S.srcOn[j]) continue;
+        const int e = s->element_of_cell[j];
+        if (grad_phase) grad_phase[e] += gphi[j];
+        if (grad_amp) grad_amp[e] += gamp[j];
+    }
+    return BD_OK;
+}
+
 /* ------------------------------------------------------------------------ */
 /* Heat + CEM43 (T:52-105)                                                   */
 /* ------------------------------------------------------------------------ */
@@ -432,6 +608,12 @@ bd_status bdo_westervelt_run(const bd_grid* g, const bd_medium* m, const bd_sour
                              const bd_westervelt_params* p, bd_westervelt_outputs* o) {
     if (p->precision == BD_F32) return wv_run<float>(g, m, s, p, o);
     return wv_run<double>(g, m, s, p, o);
+}
+
+bd_status bdo_westervelt_adjoint(const bd_grid* g, const bd_medium* m, const bd_source* s,
+                                 const bd_westervelt_params* p, const bd_focal_loss* loss, double* loss_out,
+                                 double* grad_phase, double* grad_amp) {
+    return wv_adjoint(g, m, s, p, loss, loss_out, grad_phase, grad_amp);
 }
 
 /* Heat run: T:52-105 per step with the Q shift of each step; FP64 T and dose.

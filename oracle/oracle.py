@@ -29,6 +29,8 @@ class Oracle:
         L = self.lib
         L.bdo_westervelt_run.argtypes = [P, P, P, P, P]
         L.bdo_westervelt_run.restype = C.c_int
+        L.bdo_westervelt_adjoint.argtypes = [P, P, P, P, P, P, P, P]
+        L.bdo_westervelt_adjoint.restype = C.c_int
         L.bdo_heat_run.argtypes = [P, P, P, P, C.c_int64, P, P, P, C.c_int32, P]
         L.bdo_heat_run.restype = C.c_int
         L.bdo_spiral_shifts.argtypes = [P, P, P, C.c_int64, P, P, C.c_int32]
@@ -86,6 +88,18 @@ class Oracle:
             if k in res:
                 res[k] = res[k].reshape(shp)
         return res
+
+    def westervelt_adjoint(self, prob: WesterveltProblem, loss):
+        """FP64 loss and its gradient w.r.t. element phases and amplitudes."""
+        ne = prob.source.n_elements
+        gp = np.zeros(ne, np.float64)
+        ga = np.zeros(ne, np.float64)
+        L = C.c_double(0.0)
+        st = self.lib.bdo_westervelt_adjoint(C.byref(prob.grid), C.byref(prob.medium), C.byref(prob.source),
+                                             C.byref(prob.params), C.byref(loss), C.addressof(L), _ptr(gp), _ptr(ga))
+        if st != 0:
+            raise RuntimeError("oracle adjoint failed: %s" % abi.STATUS_NAMES.get(st, st))
+        return L.value, gp, ga
 
     # ---------------------------------------------------------------- T
     def heat(self, thermal, Q, sx, sy, T0, TD0, snap_steps=None):
