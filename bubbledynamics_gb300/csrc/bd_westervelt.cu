@@ -804,24 +804,30 @@ static void ck_load(WvSession& S, const void* blob, size_t bytes) {
 
 
 // ---------------------------------------------------------------- adjoint
+template <class real, int NR>
+static void adj_launch_n(WvSession& S, const AdjArgs<real>& a, cudaStream_t st) {
+    const WvConst<real>* K = S.kconst.as<WvConst<real>>();
+    constexpr int VEC = 16 / sizeof(real);
+    if (S.nx % VEC == 0) {
+        const long long nv = (long long)S.ncell / VEC;
+        adj_point_kernel<real, NR, VEC><<<(unsigned)((nv + 255) / 256), 256, 0, st>>>(a, K);
+    } else {
+        adj_point_kernel<real, NR, 1><<<(unsigned)((S.ncell + 255) / 256), 256, 0, st>>>(a, K);
+    }
+    BD_LAUNCHED(S.ctx);
+    dim3 b(32, 8), g((S.nx + 31) / 32, (S.ny + 7) / 8, (S.nz + a.zb - 1) / a.zb);
+    adj_stencil_kernel<real><<<g, b, 0, st>>>(a);
+    BD_LAUNCHED(S.ctx);
+}
+
 template <class real>
 static void adj_launch(WvSession& S, const AdjArgs<real>& a, cudaStream_t st) {
-    const WvConst<real>* K = S.kconst.as<WvConst<real>>();
-    dim3 b(32, 8), g((S.nx + 31) / 32, (S.ny + 7) / 8, S.nz);
     switch (S.max_relax) {
-        case 0: adj_pass1_kernel<real, 0><<<g, b, 0, st>>>(a, K); break;
-        case 1: adj_pass1_kernel<real, 1><<<g, b, 0, st>>>(a, K); break;
-        case 2: adj_pass1_kernel<real, 2><<<g, b, 0, st>>>(a, K); break;
-        default: adj_pass1_kernel<real, BD_MAX_RELAX><<<g, b, 0, st>>>(a, K); break;
+        case 0: adj_launch_n<real, 0>(S, a, st); break;
+        case 1: adj_launch_n<real, 1>(S, a, st); break;
+        case 2: adj_launch_n<real, 2>(S, a, st); break;
+        default: adj_launch_n<real, BD_MAX_RELAX>(S, a, st); break;
     }
-    BD_LAUNCHED(S.ctx);
-    switch (S.max_relax) {
-        case 0: adj_pass2_kernel<real, 0><<<g, b, 0, st>>>(a, K); break;
-        case 1: adj_pass2_kernel<real, 1><<<g, b, 0, st>>>(a, K); break;
-        case 2: adj_pass2_kernel<real, 2><<<g, b, 0, st>>>(a, K); break;
-        default: adj_pass2_kernel<real, BD_MAX_RELAX><<<g, b, 0, st>>>(a, K); break;
-    }
-    BD_LAUNCHED(S.ctx);
 }
 
 template <class real>
@@ -829,14 +835,32 @@ static void adjoint_solve(WvSession& S, const bd_focal_loss* loss, double* loss_
                           double* grad_amp, double* timings) {
     cudaStream_t st = S.ctx->stream;
     const int64_t N = S.p.n_steps;
-    const int64_t Kc = loss->checkpoint_every > 0 ? loss->checkpoint_every
-                                                  : std::max<int64_t>(1, (int64_t)std::ceil(std::sqrt((double)N)));
-    const int64_t nck = (N + Kc - 1) / Kc;
     const size_t f = S.ncell * S.esz;
+    const int64_t sqrtN = std::max<int64_t>(1, (int64_t)std::ceil(std::sqrt((double)N)));
+    int64_t Kc = loss->checkpoint_every > 0 ? std::min<int64_t>(loss->checkpoint_every, N) : sqrtN;
+    if (loss->checkpoint_every < 0) {
+        // the whole history when it fits in half of the free device memory
+        size_t fr = 0, tot = 0;
+        BD_CUDA(cudaMemGetInfo(&fr, &tot));
+        if ((double)(N + 5) * (double)f <= 0.5 * (double)fr) Kc = N;
+    }
+    const int64_t nck = (N + Kc - 1) / Kc;
     const int nlev = 5 + 2 * S.max_relax;
-    // forward with checkpoints at steps 0, Kc, 2Kc, ...
-    std::vector<PoolBuf> ck(std::max<int64_t>(nck, 1) * nlev);
+    // checkpoints at steps 0, Kc, ..., (nck - 2) Kc; the last segment is stored level by level
+    // during the forward itself and never recomputed
+    std::vector<PoolBuf> ck((nck - 1) * nlev);
     for (auto& b : ck) b.alloc(S.ctx, f);
+    std::vector<PoolBuf> seg(Kc + 5);   // seg[j] = p^{s0 - 4 + j} of the current segment
+    for (auto& b : seg) b.alloc(S.ctx, f);
+    auto store_segment = [&](int64_t s0, int64_t s1) {
+        for (int k = 0; k < 5; ++k)
+            BD_CUDA(cudaMemcpyAsync(seg[4 - k].p, S.P[(head_of(s0) + k) % 5].p, f, cudaMemcpyDeviceToDevice, st));
+        for (int64_t s = s0; s < s1; ++s) {
+            issue_steps(S, S.variant, s, 1, st);
+            S.step = s + 1;
+            BD_CUDA(cudaMemcpyAsync(seg[s - s0 + 5].p, S.P[head_of(s + 1)].p, f, cudaMemcpyDeviceToDevice, st));
+        }
+    };
     auto level_buf = [&](int64_t s, int k) -> PoolBuf& {   // k < 5: p^{s-k}; 5 + 2v + j: R^{s-1-j} of process v
         if (k < 5) return S.P[(head_of(s) + k) % 5];
         const int v = (k - 5) / 2, j = (k - 5) % 2;
@@ -844,10 +868,14 @@ static void adjoint_solve(WvSession& S, const bd_focal_loss* loss, double* loss_
     };
     BD_CUDA(cudaEventRecord(S.ctx->ev0, st));
     for (int64_t c = 0; c < nck; ++c) {
-        const int64_t s0 = c * Kc;
-        for (int k = 0; k < nlev; ++k)
-            BD_CUDA(cudaMemcpyAsync(ck[c * nlev + k].p, level_buf(s0, k).p, f, cudaMemcpyDeviceToDevice, st));
-        advance(S, std::min<int64_t>(Kc, N - s0), S.p.graph_chunk >= 0);
+        const int64_t s0 = c * Kc, s1 = std::min<int64_t>(N, s0 + Kc);
+        if (c + 1 < nck) {
+            for (int k = 0; k < nlev; ++k)
+                BD_CUDA(cudaMemcpyAsync(ck[c * nlev + k].p, level_buf(s0, k).p, f, cudaMemcpyDeviceToDevice, st));
+            advance(S, s1 - s0, S.p.graph_chunk >= 0);
+        } else {
+            store_segment(s0, s1);
+        }
     }
     BD_CUDA(cudaEventRecord(S.ctx->ev1, st));
     BD_CUDA(cudaEventSynchronize(S.ctx->ev1));
@@ -870,11 +898,11 @@ static void adjoint_solve(WvSession& S, const bd_focal_loss* loss, double* loss_
             }
     if (loss_out) *loss_out = L;
     // backward buffers
-    PoolBuf mu[5], muR[BD_MAX_RELAX][2], H, gphi, gamp, eamp;
+    PoolBuf mu[6], muR[BD_MAX_RELAX][3], gphi, gamp, eamp, H;
+    H.alloc(S.ctx, f);
     for (auto& b : mu) { b.alloc(S.ctx, f); BD_CUDA(cudaMemsetAsync(b.p, 0, f, st)); }
     for (int v = 0; v < S.max_relax; ++v)
         for (auto& b : muR[v]) { b.alloc(S.ctx, f); BD_CUDA(cudaMemsetAsync(b.p, 0, f, st)); }
-    H.alloc(S.ctx, f);
     gphi.alloc(S.ctx, S.plane * 8); gamp.alloc(S.ctx, S.plane * 8);
     BD_CUDA(cudaMemsetAsync(gphi.p, 0, S.plane * 8, st));
     BD_CUDA(cudaMemsetAsync(gamp.p, 0, S.plane * 8, st));
@@ -889,8 +917,6 @@ static void adjoint_solve(WvSession& S, const bd_focal_loss* loss, double* loss_
         }
     }
     upload(S, eamp, ea);
-    std::vector<PoolBuf> seg(Kc + 5);
-    for (auto& b : seg) b.alloc(S.ctx, f);
     // recompute without accumulators
     const bd_westervelt_params saved = S.p;
     S.p.peak_end = S.p.peak_start;
@@ -912,7 +938,13 @@ static void adjoint_solve(WvSession& S, const bd_focal_loss* loss, double* loss_
     a.dt = (real)S.g.dt;
     a.relax_scheme = S.p.relax_scheme;
     a.src_iz = (S.s.kind != BD_SRC_NONE) ? S.s.plane_iz : -1;
-    a.H = H.as<real>();
+    {
+        // stencil pass: about four waves of 8 CTAs per SM
+        const long long tiles = (long long)((S.nx + 31) / 32) * ((S.ny + 7) / 8);
+        const long long target = 32LL * S.ctx->sm_count;
+        a.zb = (int)std::min<long long>(64, std::max<long long>(4, (tiles * S.nz + target - 1) / target));
+        a.H = H.as<real>();
+    }
     a.gphi = gphi.as<double>(); a.gamp = gamp.as<double>(); a.e_amp = eamp.as<double>();
     a.sAf = S.sAf.as<float>(); a.sPsi = S.sPsi.as<float>(); a.sTauf = S.sTauf.as<float>();
     a.theta = S.theta.as<float>(); a.tb0 = S.tb0.as<float>();
@@ -933,33 +965,30 @@ static void adjoint_solve(WvSession& S, const bd_focal_loss* loss, double* loss_
     for (int64_t c = nck - 1; c >= 0; --c) {
         const int64_t s0 = c * Kc, s1 = std::min<int64_t>(N, s0 + Kc);
         BD_CUDA(cudaEventRecord(S.ctx->ev0, st));
-        for (int k = 0; k < nlev; ++k)
-            BD_CUDA(cudaMemcpyAsync(level_buf(s0, k).p, ck[c * nlev + k].p, f, cudaMemcpyDeviceToDevice, st));
-        long long sb = s0;
-        BD_CUDA(cudaMemcpyAsync(S.step_base.p, &sb, sizeof sb, cudaMemcpyHostToDevice, st));
-        BD_CUDA(cudaStreamSynchronize(st));
-        S.step = s0;
-        // seg[j] holds p^{s0 - 4 + j}
-        for (int k = 0; k < 5; ++k)
-            BD_CUDA(cudaMemcpyAsync(seg[4 - k].p, ck[c * nlev + k].p, f, cudaMemcpyDeviceToDevice, st));
-        for (int64_t s = s0; s < s1; ++s) {
-            issue_steps(S, S.variant, s, 1, st);
-            S.step = s + 1;
-            BD_CUDA(cudaMemcpyAsync(seg[s - s0 + 5].p, S.P[head_of(s + 1)].p, f, cudaMemcpyDeviceToDevice, st));
+        if (c + 1 < nck) {
+            for (int k = 0; k < nlev; ++k)
+                BD_CUDA(cudaMemcpyAsync(level_buf(s0, k).p, ck[c * nlev + k].p, f, cudaMemcpyDeviceToDevice, st));
+            long long sb = s0;
+            BD_CUDA(cudaMemcpyAsync(S.step_base.p, &sb, sizeof sb, cudaMemcpyHostToDevice, st));
+            BD_CUDA(cudaStreamSynchronize(st));
+            S.step = s0;
+            store_segment(s0, s1);
         }
         BD_CUDA(cudaEventRecord(S.ctx->ev1, st));
         for (int64_t s = s1 - 1; s >= s0; --s) {
-            for (int k = 0; k < 5; ++k) a.mu[k] = mu[(rot + k) % 5].as<real>();
+            for (int k = 0; k < 5; ++k) a.mu[k] = mu[(rot + k) % 6].as<real>();
+            a.mu5 = mu[(rot + 5) % 6].as<real>();
             for (int v = 0; v < S.max_relax; ++v) {
                 a.muR1[v] = muR[v][rrot].as<real>();
-                a.muR2[v] = muR[v][rrot ^ 1].as<real>();
+                a.muR2[v] = muR[v][(rrot + 1) % 3].as<real>();
+                a.muR3[v] = muR[v][(rrot + 2) % 3].as<real>();
             }
             for (int k = 0; k < 5; ++k) a.fp[k] = seg[s - s0 + 5 - k].as<real>();
             a.step = s;
             a.in_window = (s >= loss->window_start && s < loss->window_end) ? 1 : 0;
             adj_launch<real>(S, a, st);
-            rot = (rot + 1) % 5;      // lambda_k now sits in the buffer of mu_{k+1}
-            rrot ^= 1;
+            rot = (rot + 1) % 6;      // lambda_k now sits in the buffer of mu_{k+1}, lambda_4 in the spare
+            rrot = (rrot + 1) % 3;
         }
         cudaEvent_t e2;
         BD_CUDA(cudaEventCreate(&e2));

@@ -6,6 +6,14 @@
 // the adjoints lambda of the input state:
 //   lambda_k = mu_{k+1} + (d p^{s+1} / d p^{s-k})^T mu_0 + (d R^s / d p^{s-k})^T muR1
 // The loss is sum_x w_L(x) sum_{s in window} p^{s+1}(x)^2 dt.
+//
+// Two kernels per backward step.  The pointwise pass reads only its own cell
+// (16-byte vector loads, several cells per thread): it adds the loss term,
+// forms gY, gD, gE and the relaxation adjoints, writes lambda_1..lambda_4, the
+// relaxation adjoints, lambda_0 without the stencil term, and H = c^2 gY.  The
+// stencil pass then adds the transposed 6th-order Laplacian of H to lambda_0.
+// lambda_4 goes to a spare buffer (the adjoint ring has six) and the
+// relaxation adjoints rotate through three buffers per process.
 #pragma once
 
 #include "wv_kernels.cuh"
@@ -17,14 +25,17 @@ struct AdjArgs {
     int nx, ny, nz;
     long long plane;
     // adjoint ring of the output state: mu[k] = adjoint of p^{s+1-k}; lambda_k is written over mu[k+1]
-    // (k = 0..3) and lambda_4 over mu[0], so the roles rotate by one per step
+    // (k = 0..3) and lambda_4 into mu5 (the spare), so the roles rotate by one per step
     real* mu[5];
-    real* muR1[BD_MAX_RELAX];   // adjoint of R^s      (receives lambda of R^{s-2})
-    real* muR2[BD_MAX_RELAX];   // adjoint of R^{s-1}  (receives lambda of R^{s-1})
+    real* mu5;
+    const real* muR1[BD_MAX_RELAX];   // adjoint of R^s
+    real* muR2[BD_MAX_RELAX];         // adjoint of R^{s-1} (receives lambda of R^{s-1})
+    real* muR3[BD_MAX_RELAX];         // spare (receives lambda of R^{s-2})
     int max_relax;
     // forward fields: fp[0] = p^{s+1}, fp[1] = p^s, fp[2] = p^{s-1}, fp[3] = p^{s-2}, fp[4] = p^{s-3}
     const real* fp[5];
-    real* H;                    // c^2 * (adjoint of Y), read with the stencil
+    int zb;                     // z planes per CTA of the stencil pass
+    real* H;                    // c^2 (adjoint of Y)
     const float* cmap;
     const uint8_t* matmap;
     const int* plane_mat;
@@ -131,7 +142,7 @@ struct AdjLocal {
 
 template <class real, int NRMAX>
 __device__ __forceinline__ AdjLocal<real, NRMAX> adj_local(const AdjArgs<real>& a, const MatConst<real>& M, real c,
-                                                          real m0, real w, long long i) {
+                                                          real m0, real w, const real* r1, const real* r2) {
     AdjLocal<real, NRMAX> L;
     const real g = m0 * w;                          // sponge: p^{s+1} = w * p_raw
     const real c2 = c * c;
@@ -148,7 +159,7 @@ __device__ __forceinline__ AdjLocal<real, NRMAX> adj_local(const AdjArgs<real>& 
         for (int v = 0; v < NRMAX; ++v)
             if (v < M.n_relax) {
                 const real av = M.ra_num[v] * ic3;
-                mr[v] = a.muR1[v][i];
+                mr[v] = r1[v];
                 sa += av;
                 gP += real(3) * av * mr[v];
                 sam += av * mr[v];
@@ -161,7 +172,7 @@ __device__ __forceinline__ AdjLocal<real, NRMAX> adj_local(const AdjArgs<real>& 
         for (int v = 0; v < NRMAX; ++v)
             if (v < M.n_relax) {
                 const real gB = M.rb[v] * (gG + mr[v]);
-                L.lR1[v] = a.muR2[v][i] + real(4) * gB;
+                L.lR1[v] = r2[v] + real(4) * gB;
                 L.lR2[v] = -gB;
             }
         L.gD = kd * L.gY;
@@ -172,9 +183,9 @@ __device__ __forceinline__ AdjLocal<real, NRMAX> adj_local(const AdjArgs<real>& 
 #pragma unroll
         for (int v = 0; v < NRMAX; ++v)
             if (v < M.n_relax) {
-                const real gR = a.muR1[v][i] + kr * g;
+                const real gR = r1[v] + kr * g;
                 gD += M.ra_num[v] * ic3 * gR;
-                L.lR1[v] = a.muR2[v][i] + real(4) * M.rb[v] * gR;
+                L.lR1[v] = r2[v] + real(4) * M.rb[v] * gR;
                 L.lR2[v] = -M.rb[v] * gR;
             }
         L.gD = gD;
@@ -182,93 +193,193 @@ __device__ __forceinline__ AdjLocal<real, NRMAX> adj_local(const AdjArgs<real>& 
     return L;
 }
 
-// Pass 1: loss term, source-plane gradients, H = c^2 gY.
-template <class real, int NRMAX>
-__global__ void adj_pass1_kernel(const AdjArgs<real> a, const WvConst<real>* __restrict__ Kp) {
-    const int ix = blockIdx.x * blockDim.x + threadIdx.x;
-    const int iy = blockIdx.y * blockDim.y + threadIdx.y;
-    const int iz = blockIdx.z;
-    if (ix >= a.nx || iy >= a.ny) return;
-    const long long col = (long long)iy * a.nx + ix;
-    const long long i = (long long)iz * a.plane + col;
-    real m0 = a.mu[0][i];
+// VEC consecutive values through one 16-byte access (VEC = 1: scalar).
+template <class real, int VEC>
+struct Vec {
+    real v[VEC];
+};
+
+template <class real, int VEC>
+__device__ __forceinline__ Vec<real, VEC> vload(const real* p) {
+    Vec<real, VEC> r;
+    if constexpr (VEC * sizeof(real) == 16) {
+        const float4 q = __ldcs(reinterpret_cast<const float4*>(p));
+        memcpy(&r, &q, 16);
+    } else {
+#pragma unroll
+        for (int k = 0; k < VEC; ++k) r.v[k] = p[k];
+    }
+    return r;
+}
+
+template <class real, int VEC>
+__device__ __forceinline__ void vstore(real* p, const Vec<real, VEC>& r) {
+    if constexpr (VEC * sizeof(real) == 16) {
+        float4 q;
+        memcpy(&q, &r, 16);
+        *reinterpret_cast<float4*>(p) = q;
+    } else {
+#pragma unroll
+        for (int k = 0; k < VEC; ++k) p[k] = r.v[k];
+    }
+}
+
+// Pointwise pass.  Thread = VEC consecutive cells along x (nx % VEC == 0).
+template <class real, int NRMAX, int VEC>
+__global__ void __launch_bounds__(256) adj_point_kernel(const AdjArgs<real> a, const WvConst<real>* __restrict__ Kp) {
+    __shared__ MatConst<real> sM[BD_MAX_MATERIALS];
+    {
+        const int n = (int)(sizeof(sM) / sizeof(int));
+        const int* src = reinterpret_cast<const int*>(Kp->mat);
+        int* dst = reinterpret_cast<int*>(sM);
+        for (int t = threadIdx.x; t < n; t += blockDim.x) dst[t] = src[t];
+    }
+    __syncthreads();
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;   // vector index
+    const long long i0 = q * VEC;
+    if (i0 >= (long long)a.nz * a.plane) return;
+    const int iz = (int)(i0 / a.plane);
+    const long long col0 = i0 - (long long)iz * a.plane;
+    const int iy = (int)(col0 / a.nx), ix0 = (int)(col0 - (long long)iy * a.nx);
+    Vec<real, VEC> m0 = vload<real, VEC>(a.mu[0] + i0);
+    Vec<real, VEC> l0 = vload<real, VEC>(a.mu[1] + i0);
+    Vec<real, VEC> l1 = vload<real, VEC>(a.mu[2] + i0);
+    Vec<real, VEC> l2 = vload<real, VEC>(a.mu[3] + i0);
+    Vec<real, VEC> l3 = vload<real, VEC>(a.mu[4] + i0);
+    Vec<real, VEC> l4, h;
     if (a.in_window) {
-        const real wl = loss_weight(a, ix, iy, iz);
-        if (wl != real(0)) {
-            m0 += real(2) * wl * a.fp[0][i] * a.dt;
-            a.mu[0][i] = m0;
+        const bool hit = abs(iz - a.fz) * abs(iz - a.fz) <= max(a.frad2, 0) || iz == a.fz;
+        if (hit) {
+#pragma unroll
+            for (int k = 0; k < VEC; ++k) {
+                const real wl = loss_weight(a, ix0 + k, iy, iz);
+                if (wl != real(0)) m0.v[k] += real(2) * wl * a.fp[0][i0 + k] * a.dt;
+            }
         }
     }
     if (iz == a.src_iz) {
-        real S, dphi;
-        src_derivs(a, (int)col, S, dphi);
-        a.gphi[col] += (double)m0 * (double)dphi;
-        const double ea = a.e_amp[col];
-        if (ea != 0.0) a.gamp[col] += (double)m0 * (double)S / ea;
-        a.H[i] = real(0);
-        return;
+#pragma unroll
+        for (int k = 0; k < VEC; ++k) {
+            const int col = (int)col0 + k;
+            real S, dphi;
+            src_derivs(a, col, S, dphi);
+            a.gphi[col] += (double)m0.v[k] * (double)dphi;
+            const double ea = a.e_amp[col];
+            if (ea != 0.0) a.gamp[col] += (double)m0.v[k] * (double)S / ea;
+            l4.v[k] = real(0);
+            h.v[k] = real(0);
+        }
+        // the source plane takes no input from the state; its relaxation values never feed p
+        for (int v = 0; v < a.max_relax; ++v) {
+            Vec<real, VEC> z;
+#pragma unroll
+            for (int k = 0; k < VEC; ++k) z.v[k] = real(0);
+            vstore<real, VEC>(a.muR2[v] + i0, z);
+            vstore<real, VEC>(a.muR3[v] + i0, z);
+        }
+    } else {
+        const Vec<real, VEC> P0 = vload<real, VEC>(a.fp[1] + i0);
+        const Vec<real, VEC> P1 = vload<real, VEC>(a.fp[2] + i0);
+        const Vec<real, VEC> P2 = vload<real, VEC>(a.fp[3] + i0);
+        const Vec<real, VEC> P3 = vload<real, VEC>(a.fp[4] + i0);
+        Vec<real, VEC> r1[NRMAX > 0 ? NRMAX : 1], r2[NRMAX > 0 ? NRMAX : 1], o2[NRMAX > 0 ? NRMAX : 1],
+            o3[NRMAX > 0 ? NRMAX : 1];
+#pragma unroll
+        for (int v = 0; v < NRMAX; ++v) {
+            r1[v] = vload<real, VEC>(a.muR1[v] + i0);
+            r2[v] = vload<real, VEC>(a.muR2[v] + i0);
+        }
+        const real wyz = a.wx ? a.wy[iy] * a.wz[iz] : real(1);
+#pragma unroll
+        for (int k = 0; k < VEC; ++k) {
+            const long long i = i0 + k;
+            const MatConst<real>& M = sM[adj_mat(a, i, iz)];
+            const real c = adj_c(a, M, i);
+            const real w = a.wx ? a.wx[ix0 + k] * wyz : real(1);
+            real rr1[NRMAX > 0 ? NRMAX : 1], rr2[NRMAX > 0 ? NRMAX : 1];
+#pragma unroll
+            for (int v = 0; v < NRMAX; ++v) { rr1[v] = r1[v].v[k]; rr2[v] = r2[v].v[k]; }
+            const AdjLocal<real, NRMAX> L = adj_local<real, NRMAX>(a, M, c, m0.v[k], w, rr1, rr2);
+            const real p0 = P0.v[k], p1 = P1.v[k], p2 = P2.v[k], p3 = P3.v[k];
+            const real kn = M.beta2_rho / (c * c);
+            const real s3 = real(3) * p0 - real(4) * p1 + p2;
+            const real d2 = real(4) * p0 - real(5) * p1 + real(4) * p2 - p3;
+            const real gY = L.gY, gD = L.gD, gE = L.gE;
+            // Y = 2 P0 - P1 + Lap(P0) + kd Dttt + kn (s3^2/4 + P0 (2P0 - 5P1 + 4P2 - P3))
+            l0.v[k] += gY * (real(2) + kn * (real(1.5) * s3 + d2)) + real(5) * gD - real(10) * gE;
+            l1.v[k] += gY * (real(-1) + kn * (real(-2) * s3 - real(5) * p0)) - real(18) * gD + real(12) * gE;
+            l2.v[k] += gY * kn * (real(0.5) * s3 + real(4) * p0) + real(24) * gD - real(6) * gE;
+            l3.v[k] += gY * kn * (-p0) - real(14) * gD + gE;
+            l4.v[k] = real(3) * gD;
+            h.v[k] = c * c * gY;
+#pragma unroll
+            for (int v = 0; v < NRMAX; ++v) {
+                const bool on = v < M.n_relax;
+                o2[v].v[k] = on ? L.lR1[v] : real(0);
+                o3[v].v[k] = on ? L.lR2[v] : real(0);
+            }
+        }
+#pragma unroll
+        for (int v = 0; v < NRMAX; ++v) {
+            vstore<real, VEC>(a.muR2[v] + i0, o2[v]);
+            vstore<real, VEC>(a.muR3[v] + i0, o3[v]);
+        }
     }
-    const WvConst<real>& K = *Kp;
-    const MatConst<real>& M = K.mat[adj_mat(a, i, iz)];
-    const real c = adj_c(a, M, i);
-    const real w = a.wx ? a.wx[ix] * a.wy[iy] * a.wz[iz] : real(1);
-    const AdjLocal<real, NRMAX> L = adj_local<real, NRMAX>(a, M, c, m0, w, i);
-    a.H[i] = c * c * L.gY;
+    vstore<real, VEC>(a.mu[1] + i0, l0);
+    vstore<real, VEC>(a.mu[2] + i0, l1);
+    vstore<real, VEC>(a.mu[3] + i0, l2);
+    vstore<real, VEC>(a.mu[4] + i0, l3);
+    vstore<real, VEC>(a.mu5 + i0, l4);
+    vstore<real, VEC>(a.H + i0, h);
 }
 
+// Stencil pass: lambda_0 += (d Lap / d p^s)^T H, the same symmetric
+// 6th-order stencil applied to H with zero outside the grid.  Each thread
+// marches along z over a.zb planes keeping H(iz-3..iz+3) of its column in
+// registers; x / y neighbours come through the cache.
 template <class real>
-__device__ __forceinline__ real hval(const AdjArgs<real>& a, int ix, int iy, int iz) {
-    if (ix < 0 || iy < 0 || iz < 0 || ix >= a.nx || iy >= a.ny || iz >= a.nz) return real(0);
-    return a.H[(long long)iz * a.plane + (long long)iy * a.nx + ix];
-}
-
-// Pass 2: the transposed stencil on H plus the pointwise Jacobian terms.
-template <class real, int NRMAX>
-__global__ void adj_pass2_kernel(const AdjArgs<real> a, const WvConst<real>* __restrict__ Kp) {
+__global__ void __launch_bounds__(256) adj_stencil_kernel(const AdjArgs<real> a) {
     const int ix = blockIdx.x * blockDim.x + threadIdx.x;
     const int iy = blockIdx.y * blockDim.y + threadIdx.y;
-    const int iz = blockIdx.z;
     if (ix >= a.nx || iy >= a.ny) return;
-    const long long i = (long long)iz * a.plane + (long long)iy * a.nx + ix;
-    // (d Lap / d p^s)^T H: the same symmetric 6th-order stencil applied to H
-    const real h0 = a.H[i];
-    auto ax = [&](int o) { return hval(a, ix + o, iy, iz) + hval(a, ix - o, iy, iz); };
-    auto ay = [&](int o) { return hval(a, ix, iy + o, iz) + hval(a, ix, iy - o, iz); };
-    auto az = [&](int o) { return hval(a, ix, iy, iz + o) + hval(a, ix, iy, iz - o); };
-    const real sxy = real(-980) * h0 + real(270) * (ax(1) + ay(1)) - real(27) * (ax(2) + ay(2)) + real(2) * (ax(3) + ay(3));
-    const real sz = real(-490) * h0 + real(270) * az(1) - real(27) * az(2) + real(2) * az(3);
-    real lam0 = a.mu[1][i] + a.kxy180 * sxy + a.kz180 * sz;
-    real lam1 = a.mu[2][i], lam2 = a.mu[3][i], lam3 = a.mu[4][i], lam4 = real(0);
-    if (iz == a.src_iz) {
-        // the source plane takes no input from the state; its relaxation values never feed p
-        for (int v = 0; v < a.max_relax; ++v) { a.muR1[v][i] = real(0); a.muR2[v][i] = real(0); }
-    } else {
-        const WvConst<real>& K = *Kp;
-        const MatConst<real>& M = K.mat[adj_mat(a, i, iz)];
-        const real c = adj_c(a, M, i);
-        const real w = a.wx ? a.wx[ix] * a.wy[iy] * a.wz[iz] : real(1);
-        const real m0 = a.mu[0][i];
-        const AdjLocal<real, NRMAX> L = adj_local<real, NRMAX>(a, M, c, m0, w, i);
-        const real P0 = a.fp[1][i], P1 = a.fp[2][i], P2 = a.fp[3][i], P3 = a.fp[4][i];
-        const real kn = M.beta2_rho / (c * c);
-        const real s3 = real(3) * P0 - real(4) * P1 + P2;
-        const real d2 = real(4) * P0 - real(5) * P1 + real(4) * P2 - P3;
-        const real gY = L.gY, gD = L.gD, gE = L.gE;
-        // Y = 2 P0 - P1 + Lap(P0) + kd Dttt + kn (s3^2/4 + P0 (2P0 - 5P1 + 4P2 - P3))
-        lam0 += gY * (real(2) + kn * (real(1.5) * s3 + d2)) + real(5) * gD - real(10) * gE;
-        lam1 += gY * (real(-1) + kn * (real(-2) * s3 - real(5) * P0)) - real(18) * gD + real(12) * gE;
-        lam2 += gY * kn * (real(0.5) * s3 + real(4) * P0) + real(24) * gD - real(6) * gE;
-        lam3 += gY * kn * (-P0) - real(14) * gD + gE;
-        lam4 = real(3) * gD;
+    const int z0 = blockIdx.z * a.zb;
+    const int z1 = min(a.nz, z0 + a.zb);
+    const long long col = (long long)iy * a.nx + ix;
+    const real* __restrict__ H = a.H;
+    real* __restrict__ lam = a.mu[1];
+    real w[7];
 #pragma unroll
-        for (int v = 0; v < NRMAX; ++v)
-            if (v < M.n_relax) { a.muR2[v][i] = L.lR1[v]; a.muR1[v][i] = L.lR2[v]; }
+    for (int k = 0; k < 6; ++k) {
+        const int z = z0 - 3 + k;
+        w[k] = (z >= 0 && z < a.nz) ? __ldg(H + (long long)z * a.plane + col) : real(0);
     }
-    a.mu[1][i] = lam0;
-    a.mu[2][i] = lam1;
-    a.mu[3][i] = lam2;
-    a.mu[4][i] = lam3;
-    a.mu[0][i] = lam4;
+    const bool xin = ix >= 3 && ix + 3 < a.nx, yin = iy >= 3 && iy + 3 < a.ny;
+    for (int iz = z0; iz < z1; ++iz) {
+        w[6] = (iz + 3 < a.nz) ? __ldg(H + (long long)(iz + 3) * a.plane + col) : real(0);
+        const real* P = H + (long long)iz * a.plane + col;
+        real ax1, ax2, ax3, ay1, ay2, ay3;
+        if (xin) {
+            ax1 = __ldg(P + 1) + __ldg(P - 1); ax2 = __ldg(P + 2) + __ldg(P - 2); ax3 = __ldg(P + 3) + __ldg(P - 3);
+        } else {
+            auto hx = [&](int o) { const int j = ix + o; return (j >= 0 && j < a.nx) ? __ldg(P + o) : real(0); };
+            ax1 = hx(1) + hx(-1); ax2 = hx(2) + hx(-2); ax3 = hx(3) + hx(-3);
+        }
+        const long long nx = a.nx;
+        if (yin) {
+            ay1 = __ldg(P + nx) + __ldg(P - nx); ay2 = __ldg(P + 2 * nx) + __ldg(P - 2 * nx);
+            ay3 = __ldg(P + 3 * nx) + __ldg(P - 3 * nx);
+        } else {
+            auto hy = [&](int o) { const int j = iy + o; return (j >= 0 && j < a.ny) ? __ldg(P + o * nx) : real(0); };
+            ay1 = hy(1) + hy(-1); ay2 = hy(2) + hy(-2); ay3 = hy(3) + hy(-3);
+        }
+        const real h0 = w[3];
+        const real sxy = real(-980) * h0 + real(270) * (ax1 + ay1) - real(27) * (ax2 + ay2) + real(2) * (ax3 + ay3);
+        const real sz = real(-490) * h0 + real(270) * (w[4] + w[2]) - real(27) * (w[5] + w[1]) + real(2) * (w[6] + w[0]);
+        const long long i = (long long)iz * a.plane + col;
+        lam[i] = lam[i] + a.kxy180 * sxy + a.kz180 * sz;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) w[k] = w[k + 1];
+    }
 }
 
 }  // namespace bd

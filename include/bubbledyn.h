@@ -234,7 +234,9 @@ typedef struct bd_focal_loss {
     int32_t focus_ix, focus_iy, focus_iz;
     int32_t focal_radius;
     int32_t side_radius;
-    int32_t checkpoint_every;           /* forward checkpoint interval (0 = ceil(sqrt(n_steps))) */
+    int32_t checkpoint_every;           /* forward checkpoint interval: 0 = ceil(sqrt(n_steps));
+                                           < 0 = keep the whole history in device memory when it
+                                           fits in half of the free memory, else ceil(sqrt(n_steps)) */
     double side_weight;
     int64_t window_start, window_end;   /* step window [start, end) */
 } bd_focal_loss;

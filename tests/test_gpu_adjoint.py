@@ -62,7 +62,7 @@ def test_adjoint_f64_vs_central_fd_16_elements(ctx):
 def test_adjoint_gradient_independent_of_checkpoint_interval(ctx, prec):
     prob, loss = presets.adjoint_mini(precision=prec)
     ref = None
-    for k in (0, 1, 7, prob.params.n_steps):
+    for k in (0, 1, 7, prob.params.n_steps, -1):
         loss.checkpoint_every = k
         L, gp, ga, _ = ctx.westervelt_adjoint(prob, loss)
         if ref is None:
