@@ -270,9 +270,52 @@ def run_westervelt(args, world, rank, local):
         "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk.summary(),
         "gpu_launches": int(launches),
     }
+    if not args.no_extra:
+        line["adjoint"] = adjoint_summary(ctx)
+        line["gilmore"] = gilmore_summary(ctx)
     if rank == 0:
         print(json.dumps(line), flush=True)
     ctx.close()
+
+
+def adjoint_summary(ctx):
+    """cfg4: forward solve vs loss + gradient, sqrt(N) checkpoints and whole history."""
+    from bubbledynamics_gb300 import presets
+    prob, loss = presets.cfg4()
+    n = prob.params.n_steps
+    fwd = ctx.westervelt(prob, want=("energy",))             # warm (autotune, allocation)
+    fwd = ctx.westervelt(prob, want=("energy",))
+    out = {"workload": "cfg4 adjoint FP32 192^3, 3 slabs, 256-element cap array, %d steps" % n,
+           "forward_ms": fwd["elapsed_ms"]}
+    for name, k in (("sqrtN", 0), ("history", -1)):
+        loss.checkpoint_every = k
+        L, gp, ga, tm = ctx.westervelt_adjoint(prob, loss)
+        tot = tm["forward_ms"] + tm["recompute_ms"] + tm["backward_ms"]
+        out[name] = {"total_ms": tot, "forward_ms": tm["forward_ms"], "recompute_ms": tm["recompute_ms"],
+                     "backward_ms": tm["backward_ms"], "ratio": tot / fwd["elapsed_ms"]}
+    out["backward_us_per_step"] = out["history"]["backward_ms"] * 1e3 / n
+    out["loss"] = L
+    return out
+
+
+def gilmore_summary(ctx, n=1 << 16, t_end=2e-6):
+    """cfg2 bubbles (first n of the 2^20 set) over a bounded window."""
+    import numpy as np
+    from bubbledynamics_gb300 import abi, presets
+    med = presets.cfg2_medium()
+    b = presets.cfg2_bubbles(1 << 20)[:n]
+    out = {"workload": "cfg2 Gilmore FP64, first %d of the 2^20 seeded bubbles, t = 0..%g s, rtol 1e-8" % (n, t_end)}
+    for name, sched in (("persistent", abi.BD_SCHEDULE_PERSISTENT), ("static", abi.BD_SCHEDULE_STATIC)):
+        o = presets.cfg2_ode(t_end=t_end)
+        o.schedule = sched
+        r, ms = ctx.gilmore(med, b, o)
+        att = float(r["n_accept"].sum() + r["n_reject"].sum())
+        out[name] = {"ms": ms, "bubbles_per_s": n / (ms * 1e-3), "attempts_per_s": att / (ms * 1e-3),
+                     "bubble_us_per_s": n * t_end * 1e6 / (ms * 1e-3)}
+    acc = r["n_accept"].astype(np.float64)
+    out["accepted_steps"] = {"mean": float(acc.mean()), "max": float(acc.max())}
+    out["speedup_vs_static"] = out["static"]["ms"] / out["persistent"]["ms"]
+    return out
 
 
 def main():
@@ -284,6 +327,7 @@ def main():
     ap.add_argument("--workload", default="westervelt", choices=["westervelt"])
     ap.add_argument("--cpu-sample", type=int, default=60)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-extra", action="store_true", help="skip the adjoint and Gilmore summaries")
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if args.impl == "reference":

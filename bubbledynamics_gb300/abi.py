@@ -56,6 +56,9 @@ BD_BUBBLE_THRESHOLD = 1
 BD_BUBBLE_STEP_CAP = 2
 BD_BUBBLE_NONFINITE = 3
 
+BD_SCHEDULE_PERSISTENT = 0
+BD_SCHEDULE_STATIC = 1
+
 i32 = C.c_int32
 i64 = C.c_int64
 f64 = C.c_double
@@ -189,6 +192,7 @@ class OdeParams(C.Structure):
     _fields_ = [
         ("t_end", f64), ("h0", f64), ("atol", f64), ("rtol", f64), ("fac_max", f64),
         ("max_steps", i64), ("stop_at_threshold", i32), ("ref_arith", i32),
+        ("schedule", i32), ("pad0", i32),
     ]
 
 

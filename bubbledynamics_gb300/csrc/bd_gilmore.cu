@@ -299,12 +299,43 @@ __device__ __forceinline__ void lane_reset(Lane& L, double R0, double h0) {
     L.Rmax = R0; L.Rmin = R0; L.t_thr = -1.0; L.thr = false;
 }
 
-// Forward integration of every bubble; work items pulled from *counter.
+// One integration attempt of a bubble's lane; returns its final status or -1
+// while it is still running.
+__device__ __forceinline__ int lane_advance(const GilK& g, const OdeK& o, const Tones& d, double R0, double pin0,
+                                            Lane& L) {
+    const int max_rej_per_step = 200;
+    if (L.t >= o.t_end) return BD_BUBBLE_DONE;
+    if (L.nacc >= o.max_steps) return BD_BUBBLE_STEP_CAP;
+    const bool acc = dp_attempt(g, o, d, R0, pin0, o.t_end, L);
+    if (acc) {
+        if (!isfinite(L.R) || !isfinite(L.U)) return BD_BUBBLE_NONFINITE;
+        L.Rmax = fmax(L.Rmax, L.R);
+        L.Rmin = fmin(L.Rmin, L.R);
+        if (L.thr && L.t_thr < 0.0) L.t_thr = L.t;
+        if (L.thr && o.stop_at_threshold) return BD_BUBBLE_THRESHOLD;
+        if (L.t >= o.t_end) return BD_BUBBLE_DONE;
+    } else if (L.nrej_step > max_rej_per_step || !(L.h > 0.0) || L.t + L.h == L.t) {
+        return BD_BUBBLE_NONFINITE;   // step size collapsed: flagged, never a hang
+    }
+    return -1;
+}
+
+__device__ __forceinline__ void lane_write(const Lane& L, int status, bd_bubble_result* r_out) {
+    bd_bubble_result r;
+    r.R = L.R; r.Rdot = L.U; r.tau = L.T; r.q = L.q; r.t = L.t;
+    r.R_max = L.Rmax; r.R_min = L.Rmin; r.t_threshold = L.t_thr;
+    r.n_accept = L.nacc; r.n_reject = L.nrej;
+    r.status = status; r.threshold = L.t_thr >= 0.0 ? 1 : 0;
+    *r_out = r;
+}
+
+// Forward integration of every bubble; a lane whose bubble finishes pulls the
+// next work item from *counter, so lanes of one warp never wait for the
+// slowest bubble of a static assignment.
 __global__ void __launch_bounds__(128) gilmore_persistent_kernel(const bd_bubble* __restrict__ bubbles, long long n,
                                                                  const GilK g, const OdeK o,
                                                                  bd_bubble_result* __restrict__ res,
                                                                  unsigned long long* __restrict__ counter) {
-    const int max_rej_per_step = 200;
     Lane L;
     Tones d;
     long long item = -1;
@@ -319,34 +350,31 @@ __global__ void __launch_bounds__(128) gilmore_persistent_kernel(const bd_bubble
             pin0 = g.P0 + g.S2 / R0;
             lane_reset(L, R0, o.h0);
         }
-        int status = -1;
-        if (L.t >= o.t_end) status = BD_BUBBLE_DONE;
-        else if (L.nacc >= o.max_steps) status = BD_BUBBLE_STEP_CAP;
-        else {
-            const bool acc = dp_attempt(g, o, d, R0, pin0, o.t_end, L);
-            if (acc) {
-                if (!isfinite(L.R) || !isfinite(L.U)) status = BD_BUBBLE_NONFINITE;
-                else {
-                    L.Rmax = fmax(L.Rmax, L.R);
-                    L.Rmin = fmin(L.Rmin, L.R);
-                    if (L.thr && L.t_thr < 0.0) L.t_thr = L.t;
-                    if (L.thr && o.stop_at_threshold) status = BD_BUBBLE_THRESHOLD;
-                    else if (L.t >= o.t_end) status = BD_BUBBLE_DONE;
-                }
-            } else if (L.nrej_step > max_rej_per_step || !(L.h > 0.0) || L.t + L.h == L.t) {
-                status = BD_BUBBLE_NONFINITE;   // step size collapsed: flagged, never a hang
-            }
-        }
+        const int status = lane_advance(g, o, d, R0, pin0, L);
         if (status >= 0) {
-            bd_bubble_result r;
-            r.R = L.R; r.Rdot = L.U; r.tau = L.T; r.q = L.q; r.t = L.t;
-            r.R_max = L.Rmax; r.R_min = L.Rmin; r.t_threshold = L.t_thr;
-            r.n_accept = L.nacc; r.n_reject = L.nrej;
-            r.status = status; r.threshold = L.t_thr >= 0.0 ? 1 : 0;
-            res[item] = r;
+            lane_write(L, status, res + item);
             item = -1;
         }
     }
+}
+
+// The same integration with one thread per bubble for its whole run (the
+// static schedule that the persistent kernel is measured against).
+__global__ void __launch_bounds__(128) gilmore_static_kernel(const bd_bubble* __restrict__ bubbles, long long n,
+                                                             const GilK g, const OdeK o,
+                                                             bd_bubble_result* __restrict__ res) {
+    const long long item = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (item >= n) return;
+    Lane L;
+    Tones d;
+    const bd_bubble& b = bubbles[item];
+    const double R0 = b.R0;
+    load_tones(b, d);
+    const double pin0 = g.P0 + g.S2 / R0;
+    lane_reset(L, R0, o.h0);
+    int status = -1;
+    while (status < 0) status = lane_advance(g, o, d, R0, pin0, L);
+    lane_write(L, status, res + item);
 }
 
 // Threshold search of G:323-429 as a per-lane state machine around one
@@ -483,6 +511,11 @@ static void launch_run(bd_context* ctx, const bd_gilmore_medium* m, long long n,
                        cudaStream_t st) {
     const GilK g = make_gilk(m);
     const OdeK o = make_odek(ode);
+    if (ode->schedule == BD_SCHEDULE_STATIC) {
+        gilmore_static_kernel<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(d_b, n, g, o, d_r);
+        BD_LAUNCHED(ctx);
+        return;
+    }
     BD_CUDA(cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), st));
     const int grid = persistent_grid(ctx, (const void*)gilmore_persistent_kernel);
     gilmore_persistent_kernel<<<grid, 128, 0, st>>>(d_b, n, g, o, d_r, d_counter);

@@ -387,7 +387,14 @@ typedef struct bd_ode_params {
     int64_t max_steps;          /* per-bubble attempt cap (flagged, never a hang) */
     int32_t stop_at_threshold;  /* 1: stop when R' <= -C_inf (G:313) */
     int32_t ref_arith;          /* 1: evaluate the RHS in the reference's operation order (no FSAL) */
+    int32_t schedule;           /* bd_schedule: persistent work-stealing lanes (default) or static */
+    int32_t pad0;
 } bd_ode_params;
+
+typedef enum bd_schedule {
+    BD_SCHEDULE_PERSISTENT = 0, /* lanes pull the next bubble when theirs finishes */
+    BD_SCHEDULE_STATIC = 1      /* one thread per bubble for its whole run (comparison baseline) */
+} bd_schedule;
 
 typedef enum bd_bubble_status {
     BD_BUBBLE_DONE = 0,

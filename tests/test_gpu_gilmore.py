@@ -108,3 +108,16 @@ def test_stop_at_threshold(ctx):
     hit = res["status"] == abi.BD_BUBBLE_THRESHOLD
     assert np.all(res["threshold"][hit] == 1)
     assert np.all(res["Rdot"][hit] <= -med.C_inf)
+
+
+def test_static_schedule_gives_the_same_bits_as_persistent(ctx):
+    """The persistent work-stealing kernel and the static one-thread-per-bubble
+    kernel run the same per-bubble arithmetic: identical results."""
+    med = presets.cfg2_medium()
+    b = presets.cfg2_bubbles(300, seed=7)
+    ode = presets.cfg2_ode(t_end=0.3e-6)
+    r1, _ = ctx.gilmore(med, b, ode)
+    ode.schedule = abi.BD_SCHEDULE_STATIC
+    r2, _ = ctx.gilmore(med, b, ode)
+    for k in ("R", "Rdot", "tau", "q", "t", "R_max", "R_min", "n_accept", "n_reject", "status"):
+        np.testing.assert_array_equal(r1[k], r2[k])
