@@ -273,6 +273,7 @@ def run_westervelt(args, world, rank, local):
     if not args.no_extra:
         line["adjoint"] = adjoint_summary(ctx)
         line["gilmore"] = gilmore_summary(ctx)
+        line["reference_gpu"] = reference_gpu_summary(ctx)
     if rank == 0:
         print(json.dumps(line), flush=True)
     ctx.close()
@@ -315,6 +316,59 @@ def gilmore_summary(ctx, n=1 << 16, t_end=2e-6):
     acc = r["n_accept"].astype(np.float64)
     out["accepted_steps"] = {"mean": float(acc.mean()), "max": float(acc.max())}
     out["speedup_vs_static"] = out["static"]["ms"] / out["persistent"]["ms"]
+    return out
+
+
+def reference_gpu_summary(ctx, w_steps=100, g_n=1 << 14, g_t_end=0.5e-6):
+    """The reference's own CUDA kernels (oracle/_ref/libbdref_gpu.so) against
+    this library on the same problems: W's step loop on the cfg1 grid with the
+    reference's two-layer physics, and G's DPRK_step one thread per bubble on
+    cfg2 bubbles (zero phases, G's 1e-9 tolerances) over a short window."""
+    import numpy as np
+    from bubbledynamics_gb300 import abi, presets
+    try:
+        from oracle.oracle import RefGpuLib, ref_g_cfg
+        rg = RefGpuLib()
+    except Exception as e:
+        return {"unavailable": str(e).splitlines()[0]}
+    out = {}
+    # ---- Westervelt, cfg1 grid, reference physics
+    k = presets.ref_W_constants()
+    k["Nxy"], k["Nz"] = CFG1["nx"], CFG1["nz"]
+    ms_ref, _ = rg.w_steps(k, w_steps, warm=10)
+    ncell = k["Nxy"] * k["Nxy"] * k["Nz"]
+    ref_us = ms_ref * 1e3 / w_steps
+    w = {"workload": "W step loop (Westervelt_space6 + source + Mur + 9 copies), 128x128x256, FP64, %d steps"
+                     % w_steps,
+         "reference_us_per_step": ref_us, "reference_gcells": ncell / (ref_us * 1e-6) / 1e9}
+    for name, prec in (("ours_f64_us_per_step", abi.BD_F64), ("ours_f32_us_per_step", abi.BD_F32)):
+        prob = presets.make_ref_W(k, prec)
+        prob.params.q_mode = abi.BD_Q_NONE
+        prob.params.n_dft = 0
+        s = ctx.westervelt_session(prob)
+        s.advance(10)
+        s.advance(w_steps)
+        w[name] = s.last_ms() * 1e3 / w_steps
+        s.close()
+    w["speedup_f64"] = ref_us / w["ours_f64_us_per_step"]
+    w["speedup_f32"] = ref_us / w["ours_f32_us_per_step"]
+    out["westervelt"] = w
+    # ---- Gilmore, one thread per bubble with G's DPRK_step
+    med = presets.cfg2_medium()
+    b = presets.cfg2_bubbles(1 << 20)[:g_n]
+    A = b["a"][:, 0] * np.sqrt(3.0)
+    f3 = b["f"][:, :3].copy()
+    st, counts, ms_g = rg.g_forward(ref_g_cfg(med), b["R0"], A, f3, g_t_end, max_steps=10 ** 8)
+    bz = b.copy()
+    bz["phi"] = 0.0
+    o = presets.cfg2_ode(t_end=g_t_end, atol=1e-9, rtol=1e-9)
+    res, ms_o = ctx.gilmore(med, bz, o)
+    out["gilmore"] = {
+        "workload": "first %d cfg2 bubbles, zero phases, t = 0..%g s, atol = rtol = 1e-9 (G:214-215)" % (g_n, g_t_end),
+        "reference_ms": ms_g, "ours_ms": ms_o, "speedup": ms_g / ms_o,
+        "reference_steps_mean": float(counts.mean()), "ours_steps_mean": float(res["n_accept"].mean()),
+        "R_rel_diff_median": float(np.median(np.abs(res["R"] - st[:, 1]) / st[:, 1])),
+    }
     return out
 
 

@@ -110,6 +110,28 @@ def build_ref(force=False):
     return REF_SO
 
 
+REF_GPU_SO = os.path.join(REF_OUT, "libbdref_gpu.so")
+
+
+def build_ref_gpu(force=False):
+    """Build oracle/_ref/libbdref_gpu.so: the reference's W and G kernel
+    sections compiled by nvcc for sm_103a with the host loops of
+    ref_gpu_harness.cu.  Returns its path, or None without the sections."""
+    src_dir = os.path.join(REF_OUT, "src")
+    if have_reference_sources():
+        extract_reference()
+    incs = [os.path.join(src_dir, "%s_kernels.inc" % k) for k in ("W", "G")]
+    if not all(os.path.exists(p) for p in incs):
+        return None
+    harness = os.path.join(HERE, "ref_gpu_harness.cu")
+    if force or not _newer(REF_GPU_SO, incs + [harness]):
+        nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+        _run([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17", "-shared",
+              "-Xcompiler", "-fPIC", "-diag-suppress", "177,550", "-I", HERE, "-o", REF_GPU_SO, harness])
+    return REF_GPU_SO
+
+
 if __name__ == "__main__":
     print(build_oracle(force="--force" in sys.argv))
     print(build_ref(force="--force" in sys.argv))
+    print(build_ref_gpu(force="--force" in sys.argv))

@@ -237,10 +237,11 @@ class RefLib:
         shp = (k["Nz"], k["Nxy"], k["Nxy"])
         return Psnap.reshape(shp), Q.reshape(shp), steps
 
-    def w_steps(self, k, n_steps):
+    def w_steps(self, k, n_steps, init=None):
         c = ref_w_cfg(k, False)
         n = k["Nxy"] * k["Nxy"] * k["Nz"]
-        state = np.zeros((12, n), np.float64)
+        state = (np.zeros((12, n), np.float64) if init is None
+                 else np.ascontiguousarray(init, dtype=np.float64).reshape(12, n).copy())
         self.lib.bdref_w_steps(C.byref(c), n_steps, _ptr(state))
         return state.reshape(12, k["Nz"], k["Nxy"], k["Nxy"])
 
@@ -275,3 +276,63 @@ class RefLib:
         self.lib.bdref_g_forward(C.byref(cfg), n, _ptr(R0), _ptr(A), _ptr(f3), endT, h0, max_steps,
                                  1 if stop_at_threshold else 0, _ptr(state), _ptr(counts), _ptr(thr))
         return state, counts, thr
+
+
+def ref_g_cfg(medium, triple_fr=True):
+    """G's __device__ constants (G:13-33) from a bd_gilmore_medium."""
+    c = RefGCfg()
+    m = medium
+    c.rho, c.P0, c.S2, c.mu4, c.G4_3 = m.rho, m.P0, m.S2, m.mu4, m.G4_3
+    c.C_inf, c.lambda_, c.n, c.B, c.gamma = m.C_inf, m.lambda_, m.n, m.B, m.gamma
+    c.gamma3 = 3.0 * m.gamma
+    c.minA, c.stepA = 1e4, 1000.0
+    c.minR0, c.stepR0 = 1e-7, 1e-7
+    c.triple_fr = 1 if triple_fr else 0
+    return c
+
+
+class RefGpuLib:
+    """The reference's own CUDA kernels on the GPU (oracle/_ref/libbdref_gpu.so)."""
+
+    def __init__(self, path=None):
+        path = path or _build.build_ref_gpu()
+        if path is None or not os.path.exists(path):
+            raise FileNotFoundError("oracle/_ref/libbdref_gpu.so is not available")
+        self.lib = C.CDLL(path)
+        L = self.lib
+        L.bdref_gpu_w_steps.argtypes = [P, C.c_int64, C.c_int64, P, P, C.c_int32]
+        L.bdref_gpu_w_steps.restype = C.c_int
+        L.bdref_gpu_g_forward.argtypes = [P, C.c_int64, P, P, P, C.c_double, C.c_double, C.c_int64, P, P, P]
+        L.bdref_gpu_g_forward.restype = C.c_int
+
+    def w_steps(self, k, n_steps, warm=0, want_state=False, init=None):
+        """Runs W's loop from zero (or from `init`, 12 fields); returns (ms of
+        the timed steps, final state or None)."""
+        c = ref_w_cfg(k, False)
+        n = k["Nxy"] * k["Nxy"] * k["Nz"]
+        if init is not None:
+            state = np.ascontiguousarray(init, dtype=np.float64).reshape(12, n).copy()
+        else:
+            state = np.zeros((12, n), np.float64) if want_state else None
+        ms = C.c_double(0.0)
+        st = self.lib.bdref_gpu_w_steps(C.byref(c), warm, n_steps, C.addressof(ms), _ptr(state),
+                                        1 if init is not None else 0)
+        if st != 0:
+            raise RuntimeError("reference GPU Westervelt loop failed (%d)" % st)
+        if state is not None:
+            state = state.reshape(12, k["Nz"], k["Nxy"], k["Nxy"])
+        return ms.value, state
+
+    def g_forward(self, cfg, R0, A, f3, endT, h0=1e-13, max_steps=10 ** 7):
+        R0 = np.ascontiguousarray(R0, dtype=np.float64)
+        A = np.ascontiguousarray(A, dtype=np.float64)
+        f3 = np.ascontiguousarray(f3, dtype=np.float64).reshape(-1)
+        n = R0.size
+        state = np.zeros((n, 5), np.float64)
+        counts = np.zeros(n, np.int64)
+        ms = C.c_double(0.0)
+        st = self.lib.bdref_gpu_g_forward(C.byref(cfg), n, _ptr(R0), _ptr(A), _ptr(f3), endT, h0, max_steps,
+                                          _ptr(state), _ptr(counts), C.addressof(ms))
+        if st != 0:
+            raise RuntimeError("reference GPU Gilmore loop failed (%d)" % st)
+        return state, counts, ms.value
