@@ -372,13 +372,35 @@ def reference_gpu_summary(ctx, w_steps=100, g_n=1 << 14, g_t_end=0.5e-6):
     return out
 
 
+def run_step_kernel(args):
+    """cfg1 time steps with plain launches and a fixed tile variant (or every
+    TMA variant): microseconds per time step from the library's CUDA events.
+    The case the ncu captures of the step kernel run."""
+    from bubbledynamics_gb300 import api
+    ctx = api.Context(0)
+    variants = [args.tile_variant] if args.tile_variant >= 0 else list(range(8, 19))
+    out = {}
+    for v in variants:
+        prob = cfg1_problem()
+        prob.params.n_steps = args.time_steps
+        prob.params.graph_chunk = -1
+        prob.params.tile_variant = v
+        r = ctx.westervelt(prob, want=("peak",))
+        out[str(v)] = 1e3 * r["elapsed_ms"] / args.time_steps
+    print(json.dumps({"workload": "cfg1 step kernel, plain launches", "time_steps": args.time_steps,
+                      "us_per_step_by_variant": out}), flush=True)
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="westervelt", choices=["westervelt"])
+    ap.add_argument("--workload", default="westervelt", choices=["westervelt", "step-kernel"])
+    ap.add_argument("--time-steps", type=int, default=30, help="step-kernel workload: time steps per solve")
+    ap.add_argument("--tile-variant", type=int, default=-1, help="step-kernel workload: variant (-1: all TMA)")
     ap.add_argument("--cpu-sample", type=int, default=60)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extra", action="store_true", help="skip the adjoint and Gilmore summaries")
@@ -386,6 +408,9 @@ def main():
     world, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, world, rank)
+    elif args.workload == "step-kernel":
+        if rank == 0:
+            run_step_kernel(args)
     else:
         run_westervelt(args, world, rank, local)
     if world > 1:

@@ -117,7 +117,7 @@ struct TmaLayout {
 // BD_MAX_RELAX), ZU planes per loop iteration (one CTA barrier and one round
 // of TMA issues per ZU planes).  The cell update is cell_update(), so every variant gives the
 // same bits as the plain kernel.
-template <class real, int TX, int TY, int CPT, int NREL, int ZU>
+template <class real, int TX, int TY, int CPT, int NREL, int ZU, int FL = -1>
 __global__ void __launch_bounds__(TX* TY / CPT) wv_tma_kernel(const WvArgs<real> a,
                                                               const WvConst<real>* __restrict__ Kp, int koff,
                                                               const __grid_constant__ TmaMaps maps,
@@ -129,7 +129,9 @@ __global__ void __launch_bounds__(TX* TY / CPT) wv_tma_kernel(const WvArgs<real>
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ MatConst<real> sK[BD_MAX_MATERIALS];
     const int nrel = NREL >= 0 ? NREL : a.max_relax;
-    const bool has_c = a.cmap != nullptr;
+    // FL >= 0: bit 0 = one material everywhere, bit 1 = per-cell c map (compile-time);
+    // FL = -1: both read from the arguments
+    const bool has_c = FL >= 0 ? (FL & 2) != 0 : a.cmap != nullptr;
     real* Pring = reinterpret_cast<real*>(smem);
     unsigned char* Qring = smem + TMA_NP * L::PSLOT;
     uint64_t* barP = reinterpret_cast<uint64_t*>(Qring + TMA_NQ * L::QS);
@@ -193,7 +195,7 @@ __global__ void __launch_bounds__(TX* TY / CPT) wv_tma_kernel(const WvArgs<real>
     int own[CPT], qi[CPT];
     bool active[CPT], inbox[CPT], murxy[CPT];
     real swxy[CPT];
-    long long col[CPT];
+    int col[CPT];                                  // column index iy * nx + ix (a plane has < 2^31 cells)
 #pragma unroll
     for (int c = 0; c < CPT; ++c) {
         const int ty = tyt + c * RPT;
@@ -204,9 +206,10 @@ __global__ void __launch_bounds__(TX* TY / CPT) wv_tma_kernel(const WvArgs<real>
         inbox[c] = ix <= a.xhi && iy <= a.yhi;
         murxy[c] = (a.mur_yp && iy >= a.ny - a.L) || (a.mur_xp && ix >= a.nx - a.L);
         swxy[c] = (a.wx && active[c]) ? mul_(a.wx[ix], a.wy[iy]) : real(1);
-        col[c] = (long long)iy * a.nx + ix;
+        col[c] = iy * a.nx + ix;
     }
     real w[CPT][7];
+#pragma unroll
     for (int k = 0; k < 6; ++k) {                  // planes z0-3 .. z0+2
         waitP(k);
         const int plane = z0 - 3 + k;
@@ -223,7 +226,10 @@ __global__ void __launch_bounds__(TX* TY / CPT) wv_tma_kernel(const WvArgs<real>
     const bool do_energy = step >= a.energy_start && step < a.energy_end;
     const long long ds = step - a.dft_start;
     const bool do_dft = a.n_dft > 0 && ds >= 0 && ds < a.dft_len;
-    const bool single_mat = !a.matmap && !a.plane_mat;
+    const bool single_mat = FL >= 0 ? (FL & 1) != 0 : (!a.matmap && !a.plane_mat);
+    const bool dpdt = a.energy_mode == BD_ENERGY_DPDT2;
+    // the material of single-material problems, in registers
+    const MatConst<real> M0 = sK[0];
 
     for (int izg = z0; izg < z1; izg += ZU) {
 #pragma unroll
@@ -268,10 +274,17 @@ __global__ void __launch_bounds__(TX* TY / CPT) wv_tma_kernel(const WvArgs<real>
         const bool murz = (a.mur_zp && iz >= a.nz - a.L) || (a.mur_zm && iz < a.Lzm);
         const real wzi = a.wz ? a.wz[iz] : real(1);
         const int mplane = single_mat ? 0 : (a.plane_mat ? __ldg(a.plane_mat + iz) : 0);
+        const long long zoff = (long long)iz * a.plane;
+        real* const p4z = a.p4 + zoff;
+        real* const pkz = a.peak + zoff;
+        real* const enz = a.energy + zoff;
+        real* rolz[NRMAX > 0 ? NRMAX : 1];
+#pragma unroll
+        for (int v = 0; v < NRMAX; ++v) rolz[v] = a.rold[v] + zoff;
 #pragma unroll
         for (int c = 0; c < CPT; ++c) {
             if (!active[c]) continue;
-            const long long i = (long long)iz * a.plane + col[c];
+            const long long i = zoff + col[c];
             const int k = qi[c];
             const real q1 = q1t[k];
             real pn;
@@ -285,32 +298,49 @@ __global__ void __launch_bounds__(TX* TY / CPT) wv_tma_kernel(const WvArgs<real>
                 const real sx1 = c0[1] + c0[-1], sx2 = c0[2] + c0[-2], sx3 = c0[3] + c0[-3];
                 constexpr int W = L::PW;
                 const real sy1 = c0[W] + c0[-W], sy2 = c0[2 * W] + c0[-2 * W], sy3 = c0[3 * W] + c0[-3 * W];
-                const int m = a.matmap ? (int)__ldg(a.matmap + i) : mplane;
-                const MatConst<real>& M = sK[m];
-                const real cs = has_c ? (real)ct[k] : M.c0;
-                real rc[NRMAX > 0 ? NRMAX : 1], ro[NRMAX > 0 ? NRMAX : 1];
+                auto upd = [&](const MatConst<real>& M) -> real {
+                    const real cs = has_c ? (real)ct[k] : M.c0;
+                    real rc[NRMAX > 0 ? NRMAX : 1], ro[NRMAX > 0 ? NRMAX : 1];
 #pragma unroll
-                for (int v = 0; v < NRMAX; ++v) {
-                    if (v < M.n_relax) {
-                        rc[v] = reinterpret_cast<const real*>(Qs + (4 + v) * L::QTB)[k];
-                        ro[v] = reinterpret_cast<const real*>(Qs + (4 + NRMAX + v) * L::QTB)[k];
+                    for (int v = 0; v < NRMAX; ++v) {
+                        if (v < M.n_relax) {
+                            rc[v] = reinterpret_cast<const real*>(Qs + (4 + v) * L::QTB)[k];
+                            ro[v] = reinterpret_cast<const real*>(Qs + (4 + NRMAX + v) * L::QTB)[k];
+                        }
                     }
-                }
-                pn = cell_update<real, NRMAX>(a, M, cs, pc, sx1, sx2, sx3, sy1, sy2, sy3, w[c], q1, q2t[k], q3t[k], q4t[k], rc, ro);
+                    const real r = cell_update<real, NRMAX>(a, M, cs, pc, sx1, sx2, sx3, sy1, sy2, sy3, w[c], q1, q2t[k],
+                                                            q3t[k], q4t[k], rc, ro);
 #pragma unroll
-                for (int v = 0; v < NRMAX; ++v)
-                    if (v < M.n_relax) a.rold[v][i] = ro[v];
+                    for (int v = 0; v < NRMAX; ++v)
+                        if (v < M.n_relax) rolz[v][col[c]] = ro[v];
+                    return r;
+                };
+                if constexpr (FL >= 0 && (FL & 1)) {
+                    pn = upd(M0);
+                } else {
+                    const int m = a.matmap ? (int)__ldg(a.matmap + i) : mplane;
+                    pn = upd(sK[m]);
+                }
                 if (a.wz) pn = mul_(pn, mul_(swxy[c], wzi));
                 have = true;
             }
             if (have) {
-                a.p4[i] = pn;
+                p4z[col[c]] = pn;
                 if (!(murz || murxy[c])) {
                     if (do_peak) {
                         const real av = fabs(pn), pk = pkt[k];
-                        a.peak[i] = av > pk ? av : pk;
+                        pkz[col[c]] = av > pk ? av : pk;
                     }
-                    if (do_energy) a.energy[i] = energy_add(a, ent[k], pn, q1);
+                    if (do_energy) {
+                        real e;
+                        if (dpdt) {
+                            const real dp = div_(add_(pn, -q1), mul_(real(2.0), a.dt));
+                            e = mul_(mul_(dp, dp), a.dt);
+                        } else {
+                            e = mul_(mul_(pn, pn), a.dt);
+                        }
+                        enz[col[c]] = add_(ent[k], e);
+                    }
                     if (do_dft && iz >= a.dz_lo && iz < a.dz_hi) {
                         const long long pl = (long long)(iz - a.dz_lo) * a.plane + col[c];
                         const long long stride = (long long)(a.dz_hi - a.dz_lo) * a.plane;
