@@ -36,8 +36,9 @@ BYTES_PER_CELL = 56          # p^n..p^{n-4} 20 B, p^{n+1} 4, R 12, c 4, peak 8, 
 METRIC = "Westervelt Gcell-updates/s"
 UNIT = "Gcell-updates/s"
 # dram__bytes_read.sum + dram__bytes_write.sum of one wv_tma_kernel launch on the
-# cfg1 grid (ncu capture of the TMA step kernel; summary in profiles/)
-NCU_TRAFFIC_BYTES = 203990272
+# cfg1 grid (mean of the two launches of the ncu capture of tile variant 16;
+# summary in profiles/westervelt_cfg1_wv_tma_kernel.md)
+NCU_TRAFFIC_BYTES = 201566336
 
 
 def peaks():

@@ -217,7 +217,8 @@ __device__ __forceinline__ real cell_update(const WvArgs<real>& a, const MatCons
     const real D1 = mul_(mul_(s3, s3), real(0.25));                                                   // W:208
     const real D2 = mul_(pc, fma_(real(2), pc, fma_(real(-5), q1, fma_(real(4), q2, -q3))));          // W:209
     const real c2 = mul_(c, c);
-    const real ic2 = div_(real(1), c2);
+    const real ic = div_(real(1), c);
+    const real ic2 = mul_(ic, ic);
     const real kxy = mul_(c2, a.kxy180);
     const real kz = mul_(c2, a.kz180);
     const real kd = mul_(M.delta_2dt, ic2);
@@ -234,7 +235,7 @@ __device__ __forceinline__ real cell_update(const WvArgs<real>& a, const MatCons
         // through p^{n+1}..p^{n-3}; p^{n+1} = Y + (c dt)^2 sum_v R_v solved per cell
         const real E = fma_(real(-10), pc, fma_(real(12), q1, fma_(real(-6), q2, q3)));
         const real kr = mul_(c2, a.dt2);
-        const real ic3 = div_(ic2, c);
+        const real ic3 = mul_(ic2, ic);
         real sa = real(0), G = real(0);
         real av[NRMAX > 0 ? NRMAX : 1], bv[NRMAX > 0 ? NRMAX : 1];
 #pragma unroll
@@ -256,7 +257,7 @@ __device__ __forceinline__ real cell_update(const WvArgs<real>& a, const MatCons
         for (int v = 0; v < NRMAX; ++v) {
             if (v < M.n_relax) {
                 // W:227: R = 2dt 2 c_v tau Dttt/(2dt^3) / ((2dt+3tau) c^3) + tau (4 R1 - R2)/(2dt+3tau)
-                const real rn = fma_(mul_(mul_(M.ra_num[v], ic2), div_(real(1), c)), Dttt,
+                const real rn = fma_(mul_(mul_(M.ra_num[v], ic2), ic), Dttt,
                                      mul_(M.rb[v], fma_(real(4), rc[v], -ro[v])));
                 ro[v] = rn;
                 sumR = add_(sumR, rn);
