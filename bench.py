@@ -273,7 +273,8 @@ def run_westervelt(args, world, rank, local):
     }
     if not args.no_extra:
         line["adjoint"] = adjoint_summary(ctx)
-        line["gilmore"] = gilmore_summary(ctx)
+        line["cfg3"] = cfg3_summary(ctx)
+        line["gilmore"] = gilmore_summary(ctx, with_cpu=not args.no_cpu)
         line["reference_gpu"] = reference_gpu_summary(ctx)
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -300,13 +301,60 @@ def adjoint_summary(ctx):
     return out
 
 
-def gilmore_summary(ctx, n=1 << 16, t_end=2e-6):
-    """cfg2 bubbles (first n of the 2^20 set) over a bounded window."""
+HEAT_BYTES_PER_CELL = 28    # theta read + write 8 B, Q 4 B, dose (FP32 pair) read + write 16 B
+
+
+def cfg3_summary(ctx, sample_spots=2):
+    """cfg3: the acoustic solve (25.2 M cells, CW until ten periods after the
+    front crossed the box), the W -> T hand-off, and `sample_spots` of the 49
+    spiral spots of bioheat + CEM43 dose (2000 steps of 1 ms each)."""
+    from bubbledynamics_gb300 import pipeline, presets
+    pk, pk_kind = peaks()
+    ac = presets.cfg3_acoustic()
+    g = ac.grid
+    ncell = g.nx * g.ny * g.nz
+    t0 = time.perf_counter()
+    res = pipeline.cfg3_run(ctx, acoustic=ac, n_spots=sample_spots)
+    wall = time.perf_counter() - t0
+    n = ac.params.n_steps
+    heat_steps = res["heat_steps"]
+    heat_us = res["heat_ms"] * 1e3 / heat_steps
+    achieved = HEAT_BYTES_PER_CELL * ncell / (heat_us * 1e-6) / 1e9
+    full_steps = 49 * 2000
+    return {
+        "workload": "cfg3 liver heating, 256x256x384, FP32 Westervelt (%d steps) -> Q -> %d of 49 spots x 2000 "
+                    "heat steps (FP32 dT, double-float dose)" % (n, sample_spots),
+        "acoustic_ms": res["acoustic_ms"], "acoustic_gcells": ncell * n / (res["acoustic_ms"] * 1e-3) / 1e9,
+        "heat_ms": res["heat_ms"], "heat_steps": heat_steps, "heat_us_per_step": heat_us,
+        "heat_gcells": ncell / (heat_us * 1e-6) / 1e9,
+        "heat_roofline": {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                          "frac": achieved / pk["hbm_gbs"], "algorithmic_bytes": HEAT_BYTES_PER_CELL * ncell,
+                          "peak_kind": pk_kind},
+        "projected_full_run_s": (res["acoustic_ms"] + heat_us * full_steps * 1e-3) * 1e-3,
+        "focal_peak_mpa": float(res["peak"].max() / 1e6),
+        "T_max_C": float(res["T"].max() - 273.15), "dose_max_min": float(res["dose"].max() / 60.0),
+        "wall_s": wall,
+    }
+
+
+def gilmore_summary(ctx, n=1 << 17, t_end=0.5e-6, cpu_n=1024, with_cpu=True):
+    """cfg2 bubbles (first n of the 2^20 set) over a bounded window; the CPU
+    checker on the first cpu_n of them over the same window, all host cores."""
     import numpy as np
     from bubbledynamics_gb300 import abi, presets
     med = presets.cfg2_medium()
     b = presets.cfg2_bubbles(1 << 20)[:n]
     out = {"workload": "cfg2 Gilmore FP64, first %d of the 2^20 seeded bubbles, t = 0..%g s, rtol 1e-8" % (n, t_end)}
+    if with_cpu:
+        from oracle.oracle import Oracle
+        orc = Oracle()
+        bc = np.ascontiguousarray(b[:cpu_n])
+        t0 = time.perf_counter()
+        orc.gilmore(med, (abi.Bubble * len(bc)).from_buffer_copy(bc.tobytes()), presets.cfg2_ode(t_end=t_end))
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"bubbles_per_s": cpu_n / dt, "bubble_us_per_s": cpu_n * t_end * 1e6 / dt,
+                               "cores": orc.threads(), "kind": "port",
+                               "sample": "first %d bubbles, same window, FP64 checker (OpenMP)" % cpu_n}
     for name, sched in (("persistent", abi.BD_SCHEDULE_PERSISTENT), ("static", abi.BD_SCHEDULE_STATIC)):
         o = presets.cfg2_ode(t_end=t_end)
         o.schedule = sched
@@ -320,7 +368,7 @@ def gilmore_summary(ctx, n=1 << 16, t_end=2e-6):
     return out
 
 
-def reference_gpu_summary(ctx, w_steps=100, g_n=1 << 14, g_t_end=0.5e-6):
+def reference_gpu_summary(ctx, w_steps=100, g_n=1 << 16, g_t_end=0.1e-6):
     """The reference's own CUDA kernels (oracle/_ref/libbdref_gpu.so) against
     this library on the same problems: W's step loop on the cfg1 grid with the
     reference's two-layer physics, and G's DPRK_step one thread per bubble on
@@ -373,6 +421,21 @@ def reference_gpu_summary(ctx, w_steps=100, g_n=1 << 14, g_t_end=0.5e-6):
     return out
 
 
+def run_gilmore(args):
+    """cfg2 bubbles through one schedule: the case the Gilmore ncu captures run."""
+    from bubbledynamics_gb300 import abi, api, presets
+    ctx = api.Context(0)
+    med = presets.cfg2_medium()
+    b = presets.cfg2_bubbles(1 << 20)[:args.bubbles]
+    o = presets.cfg2_ode(t_end=args.t_end)
+    o.schedule = abi.BD_SCHEDULE_STATIC if args.schedule == "static" else abi.BD_SCHEDULE_PERSISTENT
+    r, ms = ctx.gilmore(med, b, o)
+    att = float(r["n_accept"].sum() + r["n_reject"].sum())
+    print(json.dumps({"workload": "cfg2 Gilmore sample", "bubbles": args.bubbles, "t_end": args.t_end,
+                      "schedule": args.schedule, "ms": ms, "attempts_per_s": att / (ms * 1e-3)}), flush=True)
+    ctx.close()
+
+
 def run_step_kernel(args):
     """cfg1 time steps with plain launches and a fixed tile variant (or every
     TMA variant): microseconds per time step from the library's CUDA events.
@@ -399,7 +462,10 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="westervelt", choices=["westervelt", "step-kernel"])
+    ap.add_argument("--workload", default="westervelt", choices=["westervelt", "step-kernel", "gilmore"])
+    ap.add_argument("--bubbles", type=int, default=1 << 16, help="gilmore workload: bubbles")
+    ap.add_argument("--t-end", type=float, default=2e-6, help="gilmore workload: window [s]")
+    ap.add_argument("--schedule", default="persistent", choices=["persistent", "static"])
     ap.add_argument("--time-steps", type=int, default=30, help="step-kernel workload: time steps per solve")
     ap.add_argument("--tile-variant", type=int, default=-1, help="step-kernel workload: variant (-1: all TMA)")
     ap.add_argument("--cpu-sample", type=int, default=60)
@@ -412,6 +478,9 @@ def main():
     elif args.workload == "step-kernel":
         if rank == 0:
             run_step_kernel(args)
+    elif args.workload == "gilmore":
+        if rank == 0:
+            run_gilmore(args)
     else:
         run_westervelt(args, world, rank, local)
     if world > 1:

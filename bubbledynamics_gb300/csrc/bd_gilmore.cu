@@ -670,13 +670,15 @@ static void launch_run(bd_context* ctx, const bd_gilmore_medium* m, long long n,
                        cudaStream_t st) {
     const GilK g = make_gilk(m);
     const OdeK o = make_odek(ode);
-    if (ode->schedule == BD_SCHEDULE_STATIC) {
+    const int grid = persistent_grid(ctx, (const void*)gilmore_persistent_kernel);
+    // with no more bubbles than resident lanes there is nothing to steal: full
+    // warps of the static kernel do the same work (and give the same bits)
+    if (ode->schedule == BD_SCHEDULE_STATIC || n <= (long long)grid * 128) {
         gilmore_static_kernel<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(d_b, n, g, o, d_r);
         BD_LAUNCHED(ctx);
         return;
     }
     BD_CUDA(cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), st));
-    const int grid = persistent_grid(ctx, (const void*)gilmore_persistent_kernel);
     gilmore_persistent_kernel<<<grid, 128, 0, st>>>(d_b, n, g, o, d_r, d_counter);
     BD_LAUNCHED(ctx);
 }

@@ -247,7 +247,11 @@ __device__ __forceinline__ real cell_update(const WvArgs<real>& a, const MatCons
                 G = add_(G, fma_(av[v], E, bv[v]));
             }
         }
-        pn = div_(fma_(kr, G, Y), fma_(mul_(real(-3), kr), sa, real(1)));
+        // p = num / (1 - x) with x = 3 kr sum a small: written as num + num x / (1 - x) so
+        // the (possibly approximate) division only touches the small correction
+        const real num = fma_(kr, G, Y);
+        const real x = mul_(mul_(real(3), kr), sa);
+        pn = fma_(num, div_(x, add_(real(1), -x)), num);
 #pragma unroll
         for (int v = 0; v < NRMAX; ++v)
             if (v < M.n_relax) ro[v] = fma_(av[v], fma_(real(3), pn, E), bv[v]);

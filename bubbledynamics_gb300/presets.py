@@ -628,6 +628,127 @@ def gaussian_focus_Q(shape, center, sigma_cells, q_max):
 
 
 # --------------------------------------------------------------------------
+# cfg3: liver heating along a 49-spot square spiral
+# --------------------------------------------------------------------------
+CFG3 = dict(nx=256, ny=256, nz=384, dx=0.15e-3, f=1.2e6, p0=0.11e6, F=40e-3, aperture=15e-3,
+            water_mm=10.0, sponge=20, n_spots_side=7, pitch=1.667e-3, spot_s=2.0, dt_T=1e-3)
+
+
+def liver_acoustic(f=1.2e6, c=1590.0):
+    """Liver for the acoustic solver: c 1590, rho 1060, beta 4.25, 0.5 dB/cm/MHz
+    through two fitted relaxation processes (relax_fit) on top of a water-like
+    thermoviscous term.  Returns (bd_material, alpha0 [Np/m/MHz], fit error)."""
+    from . import relax_fit as rf
+    a0 = rf.db_cm_mhz_to_np_m_mhz(0.5)
+    delta = water_delta(f, c)
+    relax, err = rf.fit_relaxation(a0, 1.0, c, delta)
+    return _material(c, 1060.0, 4.25, delta, relax=relax, absorption=a0 * f / 1e6), a0, err
+
+
+def cfg3_acoustic(nx=None, ny=None, nz=None, n_steps=None, precision=abi.BD_F32):
+    """The acoustic half of cfg3: FP32 Westervelt on 256x256x384 at dx = 0.15 mm,
+    a 10 mm water path then liver, a 1.2 MHz bowl (F = 40 mm, aperture radius
+    15 mm) continuous wave, 20-cell sponges.  The bowl's surface pressure of
+    0.11 MPa gives about 1.5 MPa at the focus (focusing gain ~14).  The energy window is
+    the last ten periods, after the wave front has crossed the box.  Smaller
+    sizes scale the geometry (tests)."""
+    k = CFG3
+    nx = nx or k["nx"]; ny = ny or k["ny"]; nz = nz or k["nz"]
+    scale = nz / k["nz"]
+    dx = k["dx"]
+    sponge = k["sponge"] if min(nx, ny, nz) >= 96 else max(4, min(nx, ny, nz) // 10)
+    g = abi.Grid()
+    g.nx, g.ny, g.nz = nx, ny, nz
+    g.x0 = -0.5 * (nx - 1) * dx
+    g.y0 = -0.5 * (ny - 1) * dx
+    g.z0 = -sponge * dx
+    g.dx = g.dz = dx
+    g.dt = 0.3 * dx / 1590.0
+    g.face[:] = [abi.BD_FACE_OPEN] * 6
+    g.sponge_cells = sponge
+    g.sponge_strength = 0.35
+    liver, a0, err = liver_acoustic(k["f"])
+    med = abi.Medium()
+    med.n_materials = 2
+    med.mat[0] = _material(1500.0, 1000.0, 3.5, water_delta(k["f"]), absorption=0.026 * (k["f"] / 1e6) ** 2)
+    med.mat[1] = liver
+    src = abi.Source()
+    src.kind = abi.BD_SRC_BOWL
+    src.plane_iz = sponge
+    F = k["F"] * scale
+    src.focal_length = F
+    src.alpha = math.atan(min(k["aperture"] * scale, 0.5 * min(nx, ny) * dx - (sponge + 2) * dx) / F)
+    src.p0 = k["p0"]
+    src.c_delay = 1500.0
+    src.n_tones = 1
+    src.freq[0] = k["f"]
+    src.amp[0] = 1.0
+    period = 1.0 / k["f"]
+    if n_steps is None:
+        t_cross = (nz * dx) / 1500.0 + 5 * period
+        n_steps = int(math.ceil(t_cross / g.dt)) + int(math.ceil(10 * period / g.dt))
+    p = _params_default(n_steps, precision)
+    p.relax_scheme = abi.BD_RELAX_SEMI_IMPLICIT
+    p.peak_start, p.peak_end = 0, n_steps
+    n_win = int(round(10 * period / g.dt))
+    p.energy_start, p.energy_end = n_steps - n_win, n_steps
+    prob = WesterveltProblem("cfg3_acoustic", g, med, src, p,
+                             meta={"f": k["f"], "alpha0": a0, "fit_error": err, "window_s": n_win * g.dt})
+    iz_liver = sponge + int(round(k["water_mm"] * 1e-3 * scale / dx))
+    prob.set_plane_material([0 if iz < iz_liver else 1 for iz in range(nz)])
+    return prob
+
+
+def square_spiral_spots(n_side, pitch_cells):
+    """Offsets (sx, sy) in cells of n_side^2 spots on a square spiral starting
+    at the centre (right, down, left, left, up, up, right x3, ...)."""
+    xs, ys = [0], [0]
+    x = y = 0
+    leg, d = 1, 0
+    dirs = [(1, 0), (0, 1), (-1, 0), (0, -1)]
+    while len(xs) < n_side * n_side:
+        for _ in range(2):
+            for _ in range(leg):
+                x += dirs[d][0]
+                y += dirs[d][1]
+                if len(xs) < n_side * n_side:
+                    xs.append(x)
+                    ys.append(y)
+            d = (d + 1) % 4
+        leg += 1
+    sx = np.round(np.array(xs) * pitch_cells).astype(np.int32)
+    sy = np.round(np.array(ys) * pitch_cells).astype(np.int32)
+    return sx, sy
+
+
+def cfg3_thermal(prob_acoustic, n_spots=None, steps_per_spot=None, precision=abi.BD_F32):
+    """The thermal half of cfg3 on the acoustic grid: water (k 0.6, rho 1000,
+    c_p 4180) then liver (k 0.52, rho 1060, c_p 3600, perfusion 0.0167 1/s),
+    37 C everywhere, dt = 1 ms, 49 spots of 2 s on a 10 mm square spiral
+    (7 x 7, 1.667 mm pitch), CEM43 dose from zero."""
+    k = CFG3
+    g = prob_acoustic.grid
+    t = abi.Thermal()
+    t.nx, t.ny, t.nz = g.nx, g.ny, g.nz
+    t.precision = precision
+    t.dx, t.dz, t.dt = g.dx, g.dz, k["dt_T"]
+    t.T_ref = 310.15
+    t.n_materials = 2
+    t.dose_init = 0
+    t.mat[0] = _thermal_material(1000.0, 4180.0, 0.6, 310.15)
+    t.mat[1] = _thermal_material(1060.0, 3600.0, 0.52, 310.15, perfusion=0.0167, T_art=310.15)
+    tr = abi.Trajectory()
+    tr.dxy, tr.dt = g.dx, k["dt_T"]
+    prob = ThermalProblem("cfg3_thermal", t, tr)
+    prob.set_plane_material(prob_acoustic.array("plane_material"))
+    sx, sy = square_spiral_spots(k["n_spots_side"], k["pitch"] / g.dx)
+    n = len(sx) if n_spots is None else n_spots
+    steps = int(round(k["spot_s"] / k["dt_T"])) if steps_per_spot is None else steps_per_spot
+    prob.set_spots(sx[:n], sy[:n], np.full(n, steps, np.int64))
+    return prob
+
+
+# --------------------------------------------------------------------------
 # Gilmore program (G:440-470) and the batched forward configuration
 # --------------------------------------------------------------------------
 def ref_G_medium():

@@ -392,7 +392,8 @@ typedef struct bd_ode_params {
 } bd_ode_params;
 
 typedef enum bd_schedule {
-    BD_SCHEDULE_PERSISTENT = 0, /* lanes pull the next bubble when theirs finishes */
+    BD_SCHEDULE_PERSISTENT = 0, /* lanes pull the next bubble when theirs finishes (batches no larger
+                                   than the resident lanes run one bubble per thread) */
     BD_SCHEDULE_STATIC = 1      /* one thread per bubble for its whole run (comparison baseline) */
 } bd_schedule;
 
