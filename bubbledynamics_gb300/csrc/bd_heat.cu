@@ -80,15 +80,12 @@ __global__ void heat_step_kernel(const HeatArgs<real> a, int koff) {
     if (z0 >= z1) return;
     real tm = __ldg(a.Tin + (long long)(z0 - 1) * a.plane + col);
     real tc = __ldg(a.Tin + (long long)z0 * a.plane + col);
-    for (int iz = z0; iz < z1; ++iz) {
+    // one cell: T:85-87 (plus the Pennes term -w dt (T - T_art), zero in the reference)
+    auto cell = [&](int iz, real tmv, real tcv, real tpv, real sxy, real q) {
         const long long i = (long long)iz * a.plane + col;
-        const real tp = __ldg(a.Tin + i + a.plane);
         const int m = a.matmap ? a.matmap[i] : (a.plane_mat ? __ldg(a.plane_mat + iz) : 0);
         const HeatMat<real>& M = a.mat[m];
-        const real q = qin ? __ldg(a.Q + (long long)iz * a.plane + colq) : real(0);   // T:76-77
-        const real sxy = __ldg(a.Tin + i - 1) + __ldg(a.Tin + i + 1) + __ldg(a.Tin + i + a.nx) + __ldg(a.Tin + i - a.nx);
-        // T:85-87 (plus the Pennes term -w dt (T - T_art), zero in the reference)
-        const real tn = tc * M.a0 + M.kxy * sxy + M.kz * (tp + tm) + M.qc * q + M.wTa;
+        const real tn = tcv * M.a0 + M.kxy * sxy + M.kz * (tpv + tmv) + M.qc * q + M.wTa;
         a.Tout[i] = tn;
         if (sizeof(real) == 8) {
             const double Tc = (double)tn - 273.15;                     // T:88
@@ -99,8 +96,31 @@ __global__ void heat_step_kernel(const HeatArgs<real> a, int koff) {
             const float inc = exp2f(x < 0.0f ? 2.0f * x : x) * (float)a.dt;
             a.TDf[i] = df_add(a.TDf[i], inc);
         }
-        tm = tc;
-        tc = tp;
+    };
+    auto sxy_at = [&](int iz) {
+        const long long i = (long long)iz * a.plane + col;
+        return __ldg(a.Tin + i - 1) + __ldg(a.Tin + i + 1) + __ldg(a.Tin + i + a.nx) + __ldg(a.Tin + i - a.nx);
+    };
+    auto q_at = [&](int iz) {                                           // T:76-77
+        return qin ? __ldg(a.Q + (long long)iz * a.plane + colq) : real(0);
+    };
+    int iz = z0;
+    // two planes per iteration: the loads of both are issued before either update
+    for (; iz + 1 < z1; iz += 2) {
+        const long long i = (long long)iz * a.plane + col;
+        const real tp0 = __ldg(a.Tin + i + a.plane);
+        const real tp1 = __ldg(a.Tin + i + 2 * a.plane);
+        const real s0 = sxy_at(iz), s1 = sxy_at(iz + 1);
+        const real q0 = q_at(iz), q1 = q_at(iz + 1);
+        cell(iz, tm, tc, tp0, s0, q0);
+        cell(iz + 1, tc, tp0, tp1, s1, q1);
+        tm = tp0;
+        tc = tp1;
+    }
+    if (iz < z1) {
+        const long long i = (long long)iz * a.plane + col;
+        const real tp = __ldg(a.Tin + i + a.plane);
+        cell(iz, tm, tc, tp, sxy_at(iz), q_at(iz));
     }
 }
 
