@@ -274,6 +274,7 @@ def run_westervelt(args, world, rank, local):
     if not args.no_extra:
         line["adjoint"] = adjoint_summary(ctx)
         line["cfg3"] = cfg3_summary(ctx)
+        line["cfg5"] = cfg5_summary(ctx)
         line["gilmore"] = gilmore_summary(ctx, with_cpu=not args.no_cpu)
         line["reference_gpu"] = reference_gpu_summary(ctx)
     if rank == 0:
@@ -337,6 +338,52 @@ def cfg3_summary(ctx, sample_spots=2):
     }
 
 
+def cfg5_summary(ctx, n_steps=4000, n_bubbles=1 << 16, t_end=0.1e-6):
+    """cfg5 at full size (512x512x768, 2 relaxation processes, three tones, the
+    9-frequency DFT over the last 10 us on the 200 planes around the focus),
+    shortened to n_steps time steps; then n_bubbles bubbles at random
+    focal-region points driven by the DFT-reconstructed local pressure."""
+    from bubbledynamics_gb300 import pipeline, presets
+    pk, pk_kind = peaks()
+    prob = presets.cfg5(n_steps=n_steps)
+    g = prob.grid
+    p = prob.params
+    ncell = g.nx * g.ny * g.nz
+    # one session: the steps before the DFT window, then the window, timed apart
+    s = ctx.westervelt_session(prob)
+    s.advance(p.dft_start)
+    out_us = s.last_ms() * 1e3 / p.dft_start
+    s.advance(p.dft_len)
+    win_ms = s.last_ms()
+    r = s.finish(want=("dft", "peak"))
+    s.close()
+    # p ring 24 B + two relaxation processes 24 B + peak 8 B (no c map; the
+    # energy accumulator only inside the window, +8 B, with the DFT's 16 B per
+    # frequency on its planes)
+    b_cell = 56
+    dft_cells = (p.dft_z_hi - p.dft_z_lo) * g.nx * g.ny
+    win_bytes = (b_cell + 8) * ncell + 16 * p.n_dft * dft_cells
+    win_us = win_ms * 1e3 / p.dft_len
+    out = {"workload": "cfg5 512x512x768 FP32, %d of 12000 steps, 9-frequency DFT over the last 10 us (530 steps) "
+                       "on %d planes; %d bubbles driven by the local field for %g s" % (n_steps, p.dft_z_hi - p.dft_z_lo,
+                                                                                         n_bubbles, t_end),
+           "us_per_step_outside_window": out_us, "gcells_outside_window": ncell / (out_us * 1e-6) / 1e9,
+           "roofline_outside_window": {"achieved": b_cell * ncell / (out_us * 1e-6) / 1e9, "peak": pk["hbm_gbs"],
+                                       "frac": b_cell * ncell / (out_us * 1e-6) / 1e9 / pk["hbm_gbs"],
+                                       "unit": "GB/s", "algorithmic_bytes_per_cell": b_cell},
+           "us_per_step_in_window": win_us,
+           "roofline_in_window": {"achieved": win_bytes / (win_us * 1e-6) / 1e9, "peak": pk["hbm_gbs"],
+                                  "frac": win_bytes / (win_us * 1e-6) / 1e9 / pk["hbm_gbs"], "unit": "GB/s"},
+           "projected_12000_steps_s": (out_us * (12000 - p.dft_len) + win_us * p.dft_len) * 1e-6,
+           "focal_peak_mpa": float(r["peak"].max() / 1e6)}
+    b, _ = pipeline.bubbles_from_dft(prob, r["dft_re"], r["dft_im"], n_bubbles)
+    res, ms = ctx.gilmore(presets.cfg2_medium(), b, presets.cfg2_ode(t_end=t_end))
+    att = float(res["n_accept"].sum() + res["n_reject"].sum())
+    out["bubbles"] = {"ms": ms, "attempts_per_s": att / (ms * 1e-3), "threshold_fraction": float(res["threshold"].mean()),
+                      "R_max_over_R0_median": float(np.median(res["R_max"] / b["R0"]))}
+    return out
+
+
 def gilmore_summary(ctx, n=1 << 17, t_end=0.5e-6, cpu_n=1024, with_cpu=True):
     """cfg2 bubbles (first n of the 2^20 set) over a bounded window; the CPU
     checker on the first cpu_n of them over the same window, all host cores."""
@@ -368,7 +415,7 @@ def gilmore_summary(ctx, n=1 << 17, t_end=0.5e-6, cpu_n=1024, with_cpu=True):
     return out
 
 
-def reference_gpu_summary(ctx, w_steps=100, g_n=1 << 16, g_t_end=0.1e-6):
+def reference_gpu_summary(ctx, w_steps=100, g_n=1 << 15, g_t_end=0.1e-6):
     """The reference's own CUDA kernels (oracle/_ref/libbdref_gpu.so) against
     this library on the same problems: W's step loop on the cfg1 grid with the
     reference's two-layer physics, and G's DPRK_step one thread per bubble on

@@ -47,3 +47,39 @@ def cfg3_run(ctx, acoustic=None, n_spots=None, steps_per_spot=None, thermal_prec
     h = ctx.heat(th.thermal, Q, th.traj)
     return {"acoustic": ac, "thermal": th, "Q": Q, "peak": r["peak"], "acoustic_ms": r["elapsed_ms"],
             "T": h["T"], "dose": h["dose"], "heat_ms": h["elapsed_ms"], "heat_steps": h["steps_done"]}
+
+
+def bubbles_from_dft(prob, dft_re, dft_im, n, seed=5, radius=2e-3, length=5e-3, R0_range=(0.5e-6, 5e-6)):
+    """n bubbles at seeded random points of the focal region (a cylinder of
+    `radius` and +-`length` around the focus), each driven by the field at its
+    cell as reconstructed from the DFT: tone j has frequency f_j, amplitude
+    2 |X_j| / N and phase arg X_j + pi/2, so that sum_j a_j sin(2 pi f_j t + phi_j)
+    is the pressure there with t = 0 at the start of the DFT window (the sample
+    phase of the accumulators is 2 pi f (s - dft_start) dt).  R0 log-uniform in
+    R0_range (the cfg2 distribution).  Returns (bubbles, cell indices)."""
+    from .api import BUBBLE_DTYPE
+    p = prob.params
+    g = prob.grid
+    rng = np.random.default_rng(seed)
+    izf = prob.meta["iz_focus"]
+    r = radius * np.sqrt(rng.uniform(0.0, 1.0, n))
+    th = rng.uniform(0.0, 2.0 * np.pi, n)
+    zz = rng.uniform(-length, length, n)
+    ix = np.clip(np.round((r * np.cos(th) - g.x0) / g.dx).astype(np.int64), 0, g.nx - 1)
+    iy = np.clip(np.round((r * np.sin(th) - g.y0) / g.dx).astype(np.int64), 0, g.ny - 1)
+    iz = np.clip(izf + np.round(zz / g.dz).astype(np.int64), p.dft_z_lo, p.dft_z_hi - 1)
+    nd = p.n_dft
+    plane = g.nx * g.ny
+    nzd = p.dft_z_hi - p.dft_z_lo
+    re = np.asarray(dft_re, dtype=np.float64).reshape(nd, nzd * plane)
+    im = np.asarray(dft_im, dtype=np.float64).reshape(nd, nzd * plane)
+    cell = (iz - p.dft_z_lo) * plane + iy * g.nx + ix
+    X = re[:, cell] + 1j * im[:, cell]                      # (nd, n)
+    b = np.zeros(n, BUBBLE_DTYPE)
+    b["R0"] = np.exp(rng.uniform(np.log(R0_range[0]), np.log(R0_range[1]), n))
+    b["n_tones"] = nd
+    for j in range(nd):
+        b["f"][:, j] = p.dft_freq[j]
+        b["a"][:, j] = 2.0 * np.abs(X[j]) / p.dft_len
+        b["phi"][:, j] = np.angle(X[j]) + 0.5 * np.pi
+    return b, (iz * plane + iy * g.nx + ix)

@@ -749,6 +749,71 @@ def cfg3_thermal(prob_acoustic, n_spots=None, steps_per_spot=None, precision=abi
 
 
 # --------------------------------------------------------------------------
+# cfg5: large nonlinear field, 9-frequency DFT, bubbles driven by the field
+# --------------------------------------------------------------------------
+CFG5 = dict(nx=512, ny=512, nz=768, dx=0.1e-3, tones=(1.0e6, 1.1e6, 1.2e6), p_tone=2.0e6, F=64e-3,
+            aperture=22e-3, sponge=20, n_steps=12000, window_s=10e-6, focal_mm=(2.0, 5.0))
+
+
+def cfg5(nx=None, ny=None, nz=None, n_steps=None, window_steps=None, precision=abi.BD_F32):
+    """Large nonlinear Westervelt: 512x512x768 at dx = 0.1 mm in liver (two
+    fitted relaxation processes), a 64 mm bowl (aperture radius 22 mm) driven
+    by 1.0 / 1.1 / 1.2 MHz, each tone about 2 MPa at the focus (bowl surface
+    2/17.5 MPa per tone, focusing gain ~17.5), 12,000 steps with dt chosen so
+    that 10 us is exactly 530 steps (CFL 0.30), and the on-the-fly DFT at the
+    three fundamentals and their 2nd and 3rd harmonics over the last 10 us, kept
+    on the planes within 10 mm of the focus.  Smaller sizes scale the geometry."""
+    k = CFG5
+    nx = nx or k["nx"]; ny = ny or k["ny"]; nz = nz or k["nz"]
+    scale = nz / k["nz"]
+    dx = k["dx"]
+    sponge = k["sponge"] if min(nx, ny, nz) >= 96 else max(4, min(nx, ny, nz) // 10)
+    spw = 530                                   # steps per 10 us
+    g = abi.Grid()
+    g.nx, g.ny, g.nz = nx, ny, nz
+    g.x0 = -0.5 * (nx - 1) * dx
+    g.y0 = -0.5 * (ny - 1) * dx
+    g.z0 = -sponge * dx
+    g.dx = g.dz = dx
+    g.dt = k["window_s"] / spw
+    g.face[:] = [abi.BD_FACE_OPEN] * 6
+    g.sponge_cells = sponge
+    g.sponge_strength = 0.35
+    liver, a0, err = liver_acoustic(1.1e6)
+    med = abi.Medium()
+    med.n_materials = 1
+    med.mat[0] = liver
+    src = abi.Source()
+    src.kind = abi.BD_SRC_BOWL
+    src.plane_iz = sponge
+    F = k["F"] * scale
+    src.focal_length = F
+    src.alpha = math.atan(min(k["aperture"] * scale, 0.5 * min(nx, ny) * dx - (sponge + 2) * dx) / F)
+    src.p0 = k["p_tone"] / 17.5
+    src.c_delay = 1590.0
+    src.n_tones = len(k["tones"])
+    for j, f in enumerate(k["tones"]):
+        src.freq[j] = f
+        src.amp[j] = 1.0
+    n_steps = n_steps or (k["n_steps"] if scale == 1.0 else int(round(k["n_steps"] * scale)))
+    n_win = window_steps or spw
+    p = _params_default(n_steps, precision)
+    p.relax_scheme = abi.BD_RELAX_SEMI_IMPLICIT
+    p.peak_start, p.peak_end = 0, n_steps
+    p.energy_start, p.energy_end = n_steps - n_win, n_steps
+    freqs = [f * h for h in (1, 2, 3) for f in k["tones"]]
+    p.n_dft = len(freqs)
+    for j, f in enumerate(freqs):
+        p.dft_freq[j] = f
+    p.dft_start, p.dft_len = n_steps - n_win, n_win
+    iz_f = sponge + int(round(F / dx))
+    half = int(round(10e-3 * scale / dx))
+    p.dft_z_lo, p.dft_z_hi = max(0, iz_f - half), min(nz, iz_f + half)
+    return WesterveltProblem("cfg5", g, med, src, p, meta={"f": 1.1e6, "iz_focus": iz_f, "fit_error": err,
+                                                            "dft_freqs": freqs})
+
+
+# --------------------------------------------------------------------------
 # Gilmore program (G:440-470) and the batched forward configuration
 # --------------------------------------------------------------------------
 def ref_G_medium():
