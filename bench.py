@@ -483,6 +483,45 @@ def run_gilmore(args):
     ctx.close()
 
 
+def run_heat(args):
+    """cfg3 heat steps on the 256x256x384 grid with a Gaussian focal source, one
+    spot: the case the heat-kernel ncu captures run."""
+    from bubbledynamics_gb300 import api, presets
+    ctx = api.Context(0)
+    ac = presets.cfg3_acoustic()
+    th = presets.cfg3_thermal(ac, n_spots=1, steps_per_spot=args.time_steps)
+    Q = presets.gaussian_focus_Q(ac.shape, (ac.meta.get("iz_focus", 287), 128, 128), (20.0, 4.0, 4.0), 1e7)
+    r = ctx.heat(th.thermal, Q, th.traj)
+    n = ac.grid.nx * ac.grid.ny * ac.grid.nz
+    print(json.dumps({"workload": "cfg3 heat steps", "steps": int(r["steps_done"]), "ms": r["elapsed_ms"],
+                      "gcells": n * r["steps_done"] / (r["elapsed_ms"] * 1e-3) / 1e9}), flush=True)
+    ctx.close()
+
+
+def run_adjoint(args):
+    """cfg4 loss + gradient over --time-steps steps (whole history): the case the
+    adjoint-kernel ncu captures run."""
+    from bubbledynamics_gb300 import api, presets
+    ctx = api.Context(0)
+    prob, loss = presets.cfg4(n_steps=args.time_steps)
+    loss.checkpoint_every = -1
+    L, gp, ga, tm = ctx.westervelt_adjoint(prob, loss)
+    print(json.dumps({"workload": "cfg4 adjoint", "time_steps": args.time_steps, "timings_ms": tm}), flush=True)
+    ctx.close()
+
+
+def run_dft(args):
+    """cfg5 physics on a 256x256x384 box with every step inside the 9-frequency
+    DFT window: the case the DFT-path ncu captures run."""
+    from bubbledynamics_gb300 import api, presets
+    ctx = api.Context(0)
+    prob = presets.cfg5(nx=256, ny=256, nz=384, n_steps=args.time_steps, window_steps=args.time_steps)
+    r = ctx.westervelt(prob, want=("dft",))
+    print(json.dumps({"workload": "cfg5 box in the DFT window", "time_steps": args.time_steps,
+                      "us_per_step": 1e3 * r["elapsed_ms"] / args.time_steps}), flush=True)
+    ctx.close()
+
+
 def run_step_kernel(args):
     """cfg1 time steps with plain launches and a fixed tile variant (or every
     TMA variant): microseconds per time step from the library's CUDA events.
@@ -509,7 +548,8 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="westervelt", choices=["westervelt", "step-kernel", "gilmore"])
+    ap.add_argument("--workload", default="westervelt",
+                    choices=["westervelt", "step-kernel", "gilmore", "heat", "adjoint", "dft"])
     ap.add_argument("--bubbles", type=int, default=1 << 16, help="gilmore workload: bubbles")
     ap.add_argument("--t-end", type=float, default=2e-6, help="gilmore workload: window [s]")
     ap.add_argument("--schedule", default="persistent", choices=["persistent", "static"])
@@ -525,9 +565,9 @@ def main():
     elif args.workload == "step-kernel":
         if rank == 0:
             run_step_kernel(args)
-    elif args.workload == "gilmore":
+    elif args.workload in ("gilmore", "heat", "adjoint", "dft"):
         if rank == 0:
-            run_gilmore(args)
+            {"gilmore": run_gilmore, "heat": run_heat, "adjoint": run_adjoint, "dft": run_dft}[args.workload](args)
     else:
         run_westervelt(args, world, rank, local)
     if world > 1:

@@ -696,7 +696,9 @@ static void setup(WvSession& S, bd_context* ctx, const bd_grid* g, const bd_medi
     } else if (S.ncell >= (1LL << 21) && p->n_steps >= 200) {
         autotune(S);
     } else {
-        S.variant = 0;
+        // short or small runs are not worth tuning: the wave-fitted TMA variant
+        // where the row pitch allows it, else the plain kernel
+        S.variant = tma_eligible(S) ? 17 : 0;
     }
 }
 

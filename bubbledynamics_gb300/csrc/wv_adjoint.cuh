@@ -335,8 +335,9 @@ __global__ void __launch_bounds__(256) adj_point_kernel(const AdjArgs<real> a, c
 
 // Stencil pass: lambda_0 += (d Lap / d p^s)^T H, the same symmetric
 // 6th-order stencil applied to H with zero outside the grid.  Each thread
-// marches along z over a.zb planes keeping H(iz-3..iz+3) of its column in
-// registers; x / y neighbours come through the cache.
+// marches along z over a.zb planes keeping H(iz-3..iz+4) of its column in
+// registers and finishes two planes per iteration, with the x / y neighbour
+// loads of both planes (through the cache) issued before either update.
 template <class real>
 __global__ void __launch_bounds__(256) adj_stencil_kernel(const AdjArgs<real> a) {
     const int ix = blockIdx.x * blockDim.x + threadIdx.x;
@@ -347,38 +348,56 @@ __global__ void __launch_bounds__(256) adj_stencil_kernel(const AdjArgs<real> a)
     const long long col = (long long)iy * a.nx + ix;
     const real* __restrict__ H = a.H;
     real* __restrict__ lam = a.mu[1];
-    real w[7];
-#pragma unroll
-    for (int k = 0; k < 6; ++k) {
-        const int z = z0 - 3 + k;
-        w[k] = (z >= 0 && z < a.nz) ? __ldg(H + (long long)z * a.plane + col) : real(0);
-    }
+    const long long nx = a.nx;
     const bool xin = ix >= 3 && ix + 3 < a.nx, yin = iy >= 3 && iy + 3 < a.ny;
-    for (int iz = z0; iz < z1; ++iz) {
-        w[6] = (iz + 3 < a.nz) ? __ldg(H + (long long)(iz + 3) * a.plane + col) : real(0);
-        const real* P = H + (long long)iz * a.plane + col;
+    auto hz = [&](int z) { return (z >= 0 && z < a.nz) ? __ldg(H + (long long)z * a.plane + col) : real(0); };
+    // sums of the +-1, +-2, +-3 neighbours along x and y on plane z
+    auto sxy = [&](int z, real& s1, real& s2, real& s3) {
+        const real* P = H + (long long)z * a.plane + col;
         real ax1, ax2, ax3, ay1, ay2, ay3;
         if (xin) {
             ax1 = __ldg(P + 1) + __ldg(P - 1); ax2 = __ldg(P + 2) + __ldg(P - 2); ax3 = __ldg(P + 3) + __ldg(P - 3);
         } else {
-            auto hx = [&](int o) { const int j = ix + o; return (j >= 0 && j < a.nx) ? __ldg(P + o) : real(0); };
+            auto hx = [&](int o) { const int jx = ix + o; return (jx >= 0 && jx < a.nx) ? __ldg(P + o) : real(0); };
             ax1 = hx(1) + hx(-1); ax2 = hx(2) + hx(-2); ax3 = hx(3) + hx(-3);
         }
-        const long long nx = a.nx;
         if (yin) {
             ay1 = __ldg(P + nx) + __ldg(P - nx); ay2 = __ldg(P + 2 * nx) + __ldg(P - 2 * nx);
             ay3 = __ldg(P + 3 * nx) + __ldg(P - 3 * nx);
         } else {
-            auto hy = [&](int o) { const int j = iy + o; return (j >= 0 && j < a.ny) ? __ldg(P + o * nx) : real(0); };
+            auto hy = [&](int o) { const int jy = iy + o; return (jy >= 0 && jy < a.ny) ? __ldg(P + o * nx) : real(0); };
             ay1 = hy(1) + hy(-1); ay2 = hy(2) + hy(-2); ay3 = hy(3) + hy(-3);
         }
+        s1 = ax1 + ay1; s2 = ax2 + ay2; s3 = ax3 + ay3;
+    };
+    auto upd = [&](int iz, const real* w, real s1, real s2, real s3, real l) {
         const real h0 = w[3];
-        const real sxy = real(-980) * h0 + real(270) * (ax1 + ay1) - real(27) * (ax2 + ay2) + real(2) * (ax3 + ay3);
+        const real sxyv = real(-980) * h0 + real(270) * s1 - real(27) * s2 + real(2) * s3;
         const real sz = real(-490) * h0 + real(270) * (w[4] + w[2]) - real(27) * (w[5] + w[1]) + real(2) * (w[6] + w[0]);
-        const long long i = (long long)iz * a.plane + col;
-        lam[i] = lam[i] + a.kxy180 * sxy + a.kz180 * sz;
+        lam[(long long)iz * a.plane + col] = l + a.kxy180 * sxyv + a.kz180 * sz;
+    };
+    real w[8];
 #pragma unroll
-        for (int k = 0; k < 6; ++k) w[k] = w[k + 1];
+    for (int k = 0; k < 6; ++k) w[k] = hz(z0 - 3 + k);
+    int iz = z0;
+    for (; iz + 1 < z1; iz += 2) {
+        w[6] = hz(iz + 3);
+        w[7] = hz(iz + 4);
+        real a1, a2, a3, b1, b2, b3;
+        sxy(iz, a1, a2, a3);
+        sxy(iz + 1, b1, b2, b3);
+        const real l0 = lam[(long long)iz * a.plane + col];
+        const real l1 = lam[(long long)(iz + 1) * a.plane + col];
+        upd(iz, w, a1, a2, a3, l0);
+        upd(iz + 1, w + 1, b1, b2, b3, l1);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) w[k] = w[k + 2];
+    }
+    if (iz < z1) {
+        w[6] = hz(iz + 3);
+        real a1, a2, a3;
+        sxy(iz, a1, a2, a3);
+        upd(iz, w, a1, a2, a3, lam[(long long)iz * a.plane + col]);
     }
 }
 

@@ -345,9 +345,23 @@ __global__ void __launch_bounds__(TX* TY / CPT) wv_tma_kernel(const WvArgs<real>
                         const long long pl = (long long)(iz - a.dz_lo) * a.plane + col[c];
                         const long long stride = (long long)(a.dz_hi - a.dz_lo) * a.plane;
                         const real* tw = a.tw + ds * a.n_dft * 2;
-                        for (int j = 0; j < a.n_dft; ++j) {
-                            a.dre[j * stride + pl] = fma_(pn, tw[2 * j], a.dre[j * stride + pl]);
-                            a.dim[j * stride + pl] = fma_(-pn, tw[2 * j + 1], a.dim[j * stride + pl]);
+                        real* dr = a.dre + pl;
+                        real* di = a.dim + pl;
+                        int j = 0;
+                        // four frequencies at a time: their eight loads are issued before any store
+                        for (; j + 4 <= a.n_dft; j += 4) {
+                            real r[4], m[4];
+#pragma unroll
+                            for (int u = 0; u < 4; ++u) { r[u] = dr[(j + u) * stride]; m[u] = di[(j + u) * stride]; }
+#pragma unroll
+                            for (int u = 0; u < 4; ++u) {
+                                dr[(j + u) * stride] = fma_(pn, tw[2 * (j + u)], r[u]);
+                                di[(j + u) * stride] = fma_(-pn, tw[2 * (j + u) + 1], m[u]);
+                            }
+                        }
+                        for (; j < a.n_dft; ++j) {
+                            dr[j * stride] = fma_(pn, tw[2 * j], dr[j * stride]);
+                            di[j * stride] = fma_(-pn, tw[2 * j + 1], di[j * stride]);
                         }
                     }
                 }
