@@ -78,6 +78,13 @@ struct WvSession {
     // tensor maps of the TMA variant in use (built per tile shape)
     int maps_tx = 0, maps_ty = 0;
     CUtensorMap mP0[5], mQ[5], mR[BD_MAX_RELAX][2], mC, mPeak, mEnergy;
+    // segment view (TMA variants only): the pressure levels of the next step are
+    // read from, and p^{n+1} written to, caller-chosen buffers instead of the ring
+    struct SegView {
+        bool on = false;
+        CUtensorMap p0, q[4];
+        void* out = nullptr;
+    } segv;
     std::vector<bd_material> mats;
     int n_materials = 0;
     bool has_cmap = false, has_matmap = false, has_planemat = false;
@@ -100,7 +107,7 @@ static WvArgs<real> make_args(WvSession& S, int64_t s) {
     a.p1 = S.P[(h + 1) % 5].as<real>();
     a.p2 = S.P[(h + 2) % 5].as<real>();
     a.p3 = S.P[(h + 3) % 5].as<real>();
-    a.p4 = S.P[(h + 4) % 5].as<real>();
+    a.p4 = S.segv.on ? static_cast<real*>(S.segv.out) : S.P[(h + 4) % 5].as<real>();
     const int rh = (int)(s & 1);
     for (int v = 0; v < S.max_relax; ++v) {
         a.rcur[v] = S.R[v][rh].as<real>();
@@ -254,6 +261,10 @@ static void launch_tma_t(WvSession& S, const WvArgs<real>& a, int64_t s, int kof
     const int h = head_of(s);
     maps.p0 = S.mP0[h];
     for (int k = 0; k < 4; ++k) maps.q[k] = S.mQ[(h + 1 + k) % 5];
+    if (S.segv.on) {
+        maps.p0 = S.segv.p0;
+        for (int k = 0; k < 4; ++k) maps.q[k] = S.segv.q[k];
+    }
     const int rh = (int)(s & 1);
     for (int v = 0; v < S.max_relax; ++v) { maps.rc[v] = S.mR[v][rh]; maps.ro[v] = S.mR[v][rh ^ 1]; }
     maps.peak = S.mPeak;
@@ -888,13 +899,38 @@ static void adjoint_solve(WvSession& S, const bd_focal_loss* loss, double* loss_
     for (auto& b : ck) b.alloc(S.ctx, f);
     std::vector<PoolBuf> seg(Kc + 5);   // seg[j] = p^{s0 - 4 + j} of the current segment
     for (auto& b : seg) b.alloc(S.ctx, f);
+    // TMA variants step straight through the segment store (each step reads its
+    // levels from seg and writes p^{s+1} there: no copy per step); the plain
+    // kernel updates p^{n-4} in place, so it steps the ring and copies
+    const Variant& var = kVariants[S.variant];
+    const bool seg_direct = var.tma != 0;
+    std::vector<CUtensorMap> segP0, segQ;
+    if (seg_direct) {
+        segP0.resize(seg.size());
+        segQ.resize(seg.size());
+        const bool fl = S.prec == BD_F32;
+        for (size_t j = 0; j < seg.size(); ++j) {
+            segP0[j] = make_map(S, seg[j].p, fl, var.tx + 8, var.ty + 6);
+            segQ[j] = make_map(S, seg[j].p, fl, var.tx, var.ty);
+        }
+    }
     auto store_segment = [&](int64_t s0, int64_t s1) {
         for (int k = 0; k < 5; ++k)
             BD_CUDA(cudaMemcpyAsync(seg[4 - k].p, S.P[(head_of(s0) + k) % 5].p, f, cudaMemcpyDeviceToDevice, st));
         for (int64_t s = s0; s < s1; ++s) {
-            issue_steps(S, S.variant, s, 1, st);
+            const int64_t j = s - s0;            // seg[j .. j+4] = p^{s-4} .. p^s
+            if (seg_direct) {
+                S.segv.on = true;
+                S.segv.p0 = segP0[j + 4];
+                for (int k = 0; k < 4; ++k) S.segv.q[k] = segQ[j + 3 - k];
+                S.segv.out = seg[j + 5].p;
+                issue_steps(S, S.variant, s, 1, st);
+                S.segv.on = false;
+            } else {
+                issue_steps(S, S.variant, s, 1, st);
+                BD_CUDA(cudaMemcpyAsync(seg[j + 5].p, S.P[head_of(s + 1)].p, f, cudaMemcpyDeviceToDevice, st));
+            }
             S.step = s + 1;
-            BD_CUDA(cudaMemcpyAsync(seg[s - s0 + 5].p, S.P[head_of(s + 1)].p, f, cudaMemcpyDeviceToDevice, st));
         }
     };
     auto level_buf = [&](int64_t s, int k) -> PoolBuf& {   // k < 5: p^{s-k}; 5 + 2v + j: R^{s-1-j} of process v
