@@ -59,6 +59,9 @@ BD_BUBBLE_NONFINITE = 3
 BD_SCHEDULE_PERSISTENT = 0
 BD_SCHEDULE_STATIC = 1
 
+BD_SLICE_XZ = 0
+BD_SLICE_XY = 1
+
 i32 = C.c_int32
 i64 = C.c_int64
 f64 = C.c_double

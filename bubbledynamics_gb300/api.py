@@ -76,6 +76,13 @@ def load(path=None):
                                      C.POINTER(C.c_double)])
     _sig(L, "bd_heat_run_device_noalloc", [P, P, P, P, P, P, C.c_int64, P])
     _sig(L, "bd_westervelt_adjoint", [P, P, P, P, P, P, C.POINTER(C.c_double), P, P, P])
+    _sig(L, "bd_write_q_bin", [C.c_char_p, P, C.c_int32, C.c_int32, C.c_int32, C.c_int32])
+    _sig(L, "bd_read_q_bin", [C.c_char_p, P, C.c_int64, C.POINTER(C.c_int64)])
+    _sig(L, "bd_write_q_axis_dat", [C.c_char_p, P, C.c_int32, C.c_int32, C.c_int32, C.c_double, C.c_double,
+                                    C.c_int32])
+    _sig(L, "bd_write_slice_dat", [C.c_char_p, P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+                                   C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_char_p])
+    _sig(L, "bd_write_threshold_table", [C.c_char_p, P, C.c_int64, P, C.c_int64, P, C.c_double])
     _lib = L
     return L
 
@@ -118,6 +125,48 @@ def gilmore_combos(n_fr=55, f_min=0.02e6, f_max=5.0e6):
     out = np.zeros(3 * n.value, np.float64)
     check(L.bd_gilmore_combos(n_fr, f_min, f_max, _ptr(out), n.value, C.byref(n)))
     return out.reshape(n.value, 3)
+
+
+# --------------------------------------------------------------------------
+# the reference programs' files
+# --------------------------------------------------------------------------
+def write_q_bin(path, Q, iz_first=2):
+    """W's Q3D_*.bin layout (W:778-790) of a (nz, ny, nx) field."""
+    Q = np.ascontiguousarray(Q, dtype=np.float64)
+    nz, ny, nx = Q.shape
+    check(load().bd_write_q_bin(str(path).encode(), _ptr(Q), nx, ny, nz, iz_first))
+
+
+def read_q_bin(path, n_half, nz):
+    """The quarter-domain volume T reads (T:276-279): (nz, n_half+1, n_half+1)."""
+    m = (n_half + 1) ** 2 * nz
+    out = np.zeros(m, np.float64)
+    got = C.c_int64(0)
+    check(load().bd_read_q_bin(str(path).encode(), _ptr(out), m, C.byref(got)))
+    return out.reshape(nz, n_half + 1, n_half + 1)
+
+
+def write_q_axis_dat(path, Q, z_min, dz, iz_first=2):
+    Q = np.ascontiguousarray(Q, dtype=np.float64)
+    nz, ny, nx = Q.shape
+    check(load().bd_write_q_axis_dat(str(path).encode(), _ptr(Q), nx, ny, nz, z_min, dz, iz_first))
+
+
+def write_slice_dat(path, field, orientation, fixed, rows, cols, header=None):
+    """T's slice files (T:419-448, T:576-640); rows / cols are (start, stop)."""
+    f = np.ascontiguousarray(field, dtype=np.float64)
+    nz, ny, nx = f.shape
+    check(load().bd_write_slice_dat(str(path).encode(), _ptr(f), nx, ny, nz, orientation, fixed, rows[0], rows[1],
+                                    cols[0], cols[1], header.encode() if header else None))
+
+
+def write_threshold_table(path, fr_combo, R0, results, elapsed_s):
+    """G's dR_Cinf_*.dat table (G:582-613)."""
+    fr = np.ascontiguousarray(fr_combo, dtype=np.float64).reshape(-1)
+    R0 = np.ascontiguousarray(R0, dtype=np.float64)
+    res = np.ascontiguousarray(results, dtype=np.float64).reshape(-1)
+    check(load().bd_write_threshold_table(str(path).encode(), _ptr(fr), fr.size // 3, _ptr(R0), R0.size, _ptr(res),
+                                          float(elapsed_s)))
 
 
 class Context:

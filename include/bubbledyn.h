@@ -441,6 +441,36 @@ bd_status bd_gilmore_threshold(bd_context* ctx, const bd_gilmore_medium* medium,
                                const double* R0, int64_t n_R0, int32_t ref_arith,
                                int64_t max_steps, double* results, double* elapsed_ms);
 
+/* ------------------------------------------------------------------------- */
+/* The reference programs' files (host only)                                  */
+/* ------------------------------------------------------------------------- */
+
+/* W's absorbed-power volume Q3D_*.bin (W:778-790): raw doubles of planes
+ * iz_first..nz-1 (W: 2), rows iy, columns ix; T reads it back (T:276-279). */
+bd_status bd_write_q_bin(const char* path, const double* Q, int32_t nx, int32_t ny, int32_t nz, int32_t iz_first);
+/* Reads exactly n doubles (*n_read gets what the file held, up to n). */
+bd_status bd_read_q_bin(const char* path, double* out, int64_t n, int64_t* n_read);
+/* W's on-axis power Q_Z_*.dat (W:767-775): "z(m);Q(W/m^3)", then z;Q per plane
+ * from iz_first at x = y = 0. */
+bd_status bd_write_q_axis_dat(const char* path, const double* Q, int32_t nx, int32_t ny, int32_t nz, double z_min,
+                              double dz, int32_t iz_first);
+
+typedef enum bd_slice {
+    BD_SLICE_XZ = 0,            /* rows z in [r0, r1), columns x in [c0, c1), at y = fixed (T:424-432) */
+    BD_SLICE_XY = 1             /* rows y in [r0, r1), columns x in [c0, c1), at z = fixed (T:437-445) */
+} bd_slice;
+
+/* T's temperature / dose slices (T:419-448, T:576-640): the header row
+ * (NULL: "Z=rows;X=columns" / "Y=rows;X=columns"), then one row per slice row
+ * of "value;" cells. */
+bd_status bd_write_slice_dat(const char* path, const double* field, int32_t nx, int32_t ny, int32_t nz,
+                             int32_t orientation, int32_t fixed, int32_t r0, int32_t r1, int32_t c0, int32_t c1,
+                             const char* header);
+/* G's threshold table dR_Cinf_*.dat (G:582-613): "fr1;fr2;fr3 --> R0;R0...",
+ * one row per combination (fr1;fr2;fr3;A...) and "time (s);t". */
+bd_status bd_write_threshold_table(const char* path, const double* fr_combo, int64_t n_combo, const double* R0,
+                                   int64_t n_R0, const double* results, double elapsed_s);
+
 #ifdef __cplusplus
 }
 #endif
