@@ -439,8 +439,8 @@ static void zero_state(WvSession& S) {
 
 static std::string tune_key(const WvSession& S) {
     char b[256];
-    snprintf(b, sizeof b, "%d:%d:%d:%d:%d:%d:%d:%d", S.nx, S.ny, S.nz, S.prec, S.max_relax, S.has_cmap ? 1 : 0,
-             S.any_mur ? 1 : 0, S.n_dft);
+    snprintf(b, sizeof b, "%d:%d:%d:%d:%d:%d:%d:%d:%d:%d", S.nx, S.ny, S.nz, S.prec, S.max_relax, S.has_cmap ? 1 : 0,
+             S.has_matmap ? 1 : 0, S.has_planemat ? 1 : 0, S.any_mur ? 1 : 0, S.n_dft);
     return b;
 }
 

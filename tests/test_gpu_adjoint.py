@@ -111,3 +111,29 @@ def test_autograd_function(ctx):
     with torch.no_grad():
         out2 = AdjointWestervelt.apply(phases, amps, prob, loss, ctx)
     assert out2.item() == pytest.approx(L, rel=1e-12)
+
+
+@pytest.mark.slow
+def test_cfg4_fp32_gradient_vs_fp64_central_fd_on_16_elements(ctx):
+    """The cfg4 geometry at full size (192^3, 256-element cap array, water /
+    fat / liver), shortened to 1000 steps: the FP32 adjoint gradient of 16
+    element phases against central differences of the FP64 forward solve
+    (h = 1e-3 rad).  Tolerance 1e-2 of the largest of the 16 gradients: FP32
+    forward levels and adjoint accumulation over 1000 steps."""
+    p32, loss = presets.cfg4(n_steps=1000)
+    _, gp, _, _ = ctx.westervelt_adjoint(p32, loss)
+    p64, _ = presets.cfg4(n_steps=1000, precision=abi.BD_F64)
+    ph = p64.array("element_phase")
+    am = p64.array("element_amp")
+    elems = np.argsort(-np.abs(gp))[:16]
+    h = 1e-3
+    fd = np.zeros(16)
+    for k, e in enumerate(elems):
+        v = []
+        for s in (1.0, -1.0):
+            p2 = ph.copy()
+            p2[e] += s * h
+            v.append(forward_loss(ctx, with_elements(p64, p2, am), loss))
+        fd[k] = (v[0] - v[1]) / (2 * h)
+    assert np.abs(fd).max() > 0
+    assert np.abs(gp[elems] - fd).max() <= 1e-2 * np.abs(fd).max()
