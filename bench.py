@@ -11,7 +11,7 @@ dx = 0.1875 mm, heterogeneous c, one relaxation process, 20-cell sponge, 1 MHz
              c map and source tables uploaded, peak and energy maps read back
   roofline   algorithmic bytes of the step kernel (56 B/cell) / its event-timed
              duration, against the measured HBM copy bandwidth
-  cpu_baseline  the CPU checker (OpenMP, all host cores) on a bounded sample
+  cpu_baseline  the CPU oracle (OpenMP, all host cores) on a bounded sample
 
 --impl reference times the reference's own Westervelt kernels built for the
 host (oracle/_ref) on the same grid (its two-layer physics), all host cores.
@@ -138,7 +138,7 @@ def cfg1_problem(precision=None):
 
 
 def cpu_baseline_port(sample_steps):
-    """The CPU checker on cfg1's grid for a few time steps, all host cores."""
+    """The CPU oracle on cfg1's grid for a few time steps, all host cores."""
     from bubbledynamics_gb300 import abi, presets
     from oracle.oracle import Oracle
     o = Oracle()
@@ -148,7 +148,7 @@ def cpu_baseline_port(sample_steps):
     dt = time.perf_counter() - t
     cells = CFG1["nx"] * CFG1["ny"] * CFG1["nz"] * sample_steps
     return {"value": cells / dt / 1e9, "unit": UNIT, "cores": o.threads(), "kind": "port",
-            "sample": "%d time steps of the 128x128x256 grid (FP64 checker, OpenMP), %.1f s" % (sample_steps, dt)}
+            "sample": "%d time steps of the 128x128x256 grid (FP64 oracle, OpenMP), %.1f s" % (sample_steps, dt)}
 
 
 def reference_cpu(sample_steps):
@@ -189,12 +189,12 @@ def run_reference(args, world, rank):
         value = statistics.median(vals)
         desc = ("%d time steps of W's Westervelt_space6 + source + Mur kernels and the 9-copy rotation "
                 "(W:139-236, W:62-135, W:575-584) on a 128x128x256 grid, host build, OpenMP over blocks" % sample)
-    except Exception as e:  # the reference build is unavailable: time the checker port instead
+    except Exception as e:  # the reference build is unavailable: time the oracle port instead
         kind = "port"
         cb = cpu_baseline_port(6)
         value = cb["value"]
         wall = 0.0
-        desc = "checker port (reference build unavailable: %s)" % str(e).splitlines()[0]
+        desc = "oracle port (reference build unavailable: %s)" % str(e).splitlines()[0]
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup,
@@ -386,7 +386,7 @@ def cfg5_summary(ctx, n_steps=4000, n_bubbles=1 << 16, t_end=0.1e-6):
 
 def gilmore_summary(ctx, n=1 << 17, t_end=0.5e-6, cpu_n=1024, with_cpu=True):
     """cfg2 bubbles (first n of the 2^20 set) over a bounded window; the CPU
-    checker on the first cpu_n of them over the same window, all host cores."""
+    oracle on the first cpu_n of them over the same window, all host cores."""
     import numpy as np
     from bubbledynamics_gb300 import abi, presets
     med = presets.cfg2_medium()
@@ -401,7 +401,7 @@ def gilmore_summary(ctx, n=1 << 17, t_end=0.5e-6, cpu_n=1024, with_cpu=True):
         dt = time.perf_counter() - t0
         out["cpu_baseline"] = {"bubbles_per_s": cpu_n / dt, "bubble_us_per_s": cpu_n * t_end * 1e6 / dt,
                                "cores": orc.threads(), "kind": "port",
-                               "sample": "first %d bubbles, same window, FP64 checker (OpenMP)" % cpu_n}
+                               "sample": "first %d bubbles, same window, FP64 oracle (OpenMP)" % cpu_n}
     for name, sched in (("persistent", abi.BD_SCHEDULE_PERSISTENT), ("static", abi.BD_SCHEDULE_STATIC)):
         o = presets.cfg2_ode(t_end=t_end)
         o.schedule = sched

@@ -3,7 +3,7 @@
  *
  * TEST INFRASTRUCTURE ONLY.  Nothing in the product links or calls this file;
  * it is imported by tests/, by __graft_entry__.smoke() and by the cpu_baseline
- * leg of bench.py, always as the checker or as the timed CPU baseline.
+ * leg of bench.py, always as the reference answer or as the timed CPU baseline.
  *
  * It restates, in plain FP64 C++ (OpenMP over z planes / bubbles):
  *   - the Westervelt step of W:139-236 with the source of W:62-85, the Mur

@@ -1,4 +1,4 @@
-"""Build recipe of the CPU checker.  TEST INFRASTRUCTURE ONLY.
+"""Build recipe of the CPU oracle.  TEST INFRASTRUCTURE ONLY.
 
   oracle/_build/libbdoracle.so  the FP64 restatement (bd_oracle.cpp)
   oracle/_ref/libbdref.so       the reference's own kernel code compiled for the

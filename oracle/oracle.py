@@ -1,4 +1,4 @@
-"""Python access to the CPU checker.  TEST INFRASTRUCTURE ONLY.
+"""Python access to the CPU oracle.  TEST INFRASTRUCTURE ONLY.
 
 `Oracle` wraps oracle/_build/libbdoracle.so (the FP64 restatement); `RefLib`
 wraps oracle/_ref/libbdref.so (the reference's own kernel code compiled for

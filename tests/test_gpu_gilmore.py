@@ -1,4 +1,4 @@
-"""Gilmore-Zener integrator on the GPU against the CPU checker and fixtures
+"""Gilmore-Zener integrator on the GPU against the CPU oracle and fixtures
 of the reference's own DPRK_step and threshold kernel."""
 import ctypes as C
 
@@ -57,7 +57,7 @@ def test_ref_arith_matches_reference_fixture(ctx, lib):
 
 def test_threshold_search_matches_oracle_with_step_cap(ctx, oracle):
     """The search kernel of G:323-429 with every integration capped at 300
-    accepted steps, on the GPU and in the checker: every item terminates, the
+    accepted steps, on the GPU and in the oracle: every item terminates, the
     capped integrations end as "not reached" in both, and the stage-1 amplitude
     ladder runs to the 10 MPa ceiling (result 1e7, G:383-387).  A full search
     costs 1e6-1e7 FP64 Dormand-Prince steps per item (about 300 us per step for
@@ -74,7 +74,7 @@ def test_threshold_search_matches_oracle_with_step_cap(ctx, oracle):
 
 def test_every_bubble_processed_once(ctx, oracle):
     """3000 bubbles with uneven step counts through the work-stealing queue:
-    every result row is written, and a sample matches the checker row by row."""
+    every result row is written, and a sample matches the oracle row by row."""
     med = presets.cfg2_medium()
     n = 3000
     b = presets.cfg2_bubbles(n, seed=7)

@@ -1,5 +1,5 @@
 """Bioheat + CEM43 dose on the GPU against the reference's own kernel
-(fixture) and the CPU checker."""
+(fixture) and the CPU oracle."""
 import numpy as np
 import pytest
 

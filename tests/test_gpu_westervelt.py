@@ -1,10 +1,10 @@
-"""Westervelt solver on the GPU (through the C ABI) against the CPU checker and
+"""Westervelt solver on the GPU (through the C ABI) against the CPU oracle and
 against fixtures of the reference's own code.
 
-Tolerances: FP64 fields agree with the FP64 checker to 1e-9 relative L2 (the
+Tolerances: FP64 fields agree with the FP64 oracle to 1e-9 relative L2 (the
 GPU contracts a*b+c into FMAs and uses its own sin); FP32 fields are held to
 the 1e-5 relative L2 field accuracy of the FP32 design (peak and energy
-maps), measured against the FP64 checker."""
+maps), measured against the FP64 oracle."""
 import numpy as np
 import pytest
 
@@ -66,7 +66,7 @@ def cfg1_small_oracle(oracle):
 
 
 def test_cfg1_small_f32_field_accuracy(ctx, cfg1_small_oracle):
-    """FP32 kernel vs FP64 checker on the benchmark physics (heterogeneous c,
+    """FP32 kernel vs FP64 oracle on the benchmark physics (heterogeneous c,
     relaxation, sponge, burst): output maps within 1e-5 relative L2."""
     prob64, exp = cfg1_small_oracle
     prob = presets.cfg1(48, 48, 96, 600, precision=abi.BD_F32)

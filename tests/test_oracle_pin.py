@@ -1,4 +1,4 @@
-"""The CPU checker against the reference itself: golden fixtures produced by
+"""The CPU oracle against the reference itself: golden fixtures produced by
 the reference's own kernel code (tests/golden/make_golden.py), and the live
 host build of that code when it is available."""
 import numpy as np

@@ -1,7 +1,7 @@
 """Multi-rank work split on CPU ranks (gloo, world size 2): Gilmore bubbles
 sharded by index range and gathered in order give the same rows as one rank;
 per-element gradients are summed across ranks.  The per-rank integrator here
-is the CPU checker (no GPU needed)."""
+is the CPU oracle (no GPU needed)."""
 import os
 import socket
 import tempfile
