@@ -80,6 +80,7 @@ struct WvSession {
     CUtensorMap mP0[5], mQ[5], mR[BD_MAX_RELAX][2], mC, mPeak, mEnergy;
     // segment view (TMA variants only): the pressure levels of the next step are
     // read from, and p^{n+1} written to, caller-chosen buffers instead of the ring
+    bool pdl = true;            // launch TMA step kernels with programmatic dependent launch
     struct SegView {
         bool on = false;
         CUtensorMap p0, q[4];
@@ -248,8 +249,31 @@ static void launch_tma_k(WvSession& S, const WvArgs<real>& a0, const TmaMaps& ma
     if (a.zb <= 0) a.zb = wave_fitted_zb(tiles, S.nz, (long long)S.ctx->sm_count * std::max(per_sm, 1));
     dim3 block(TX, TY / CPT, 1);
     dim3 grid((S.nx + TX - 1) / TX, (S.ny + TY - 1) / TY, (S.nz + a.zb - 1) / a.zb);
-    wv_tma_kernel<real, TX, TY, CPT, NREL, ZU, FL><<<grid, block, L::SMEM, st>>>(a, S.kconst.as<WvConst<real>>(), koff,
-                                                                             maps, S.flag.as<unsigned>() + 1);
+    const WvConst<real>* K = S.kconst.as<WvConst<real>>();
+    unsigned* errp = S.flag.as<unsigned>() + 1;
+    if (S.pdl) {
+        // programmatic dependent launch: this grid may start while the previous
+        // step's grid finishes (the kernel waits for its data)
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = grid;
+        cfg.blockDim = block;
+        cfg.dynamicSmemBytes = L::SMEM;
+        cfg.stream = st;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr[0].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        const cudaError_t e = cudaLaunchKernelEx(&cfg, wv_tma_kernel<real, TX, TY, CPT, NREL, ZU, FL>, a, K, koff, maps,
+                                                 errp);
+        if (e == cudaSuccess) {
+            BD_LAUNCHED(S.ctx);
+            return;
+        }
+        (void)cudaGetLastError();   // not available here: ordinary launches from now on
+        S.pdl = false;
+    }
+    wv_tma_kernel<real, TX, TY, CPT, NREL, ZU, FL><<<grid, block, L::SMEM, st>>>(a, K, koff, maps, errp);
     BD_LAUNCHED(S.ctx);
 }
 

@@ -143,7 +143,6 @@ __global__ void __launch_bounds__(TX* TY / CPT) wv_tma_kernel(const WvArgs<real>
     const int z0 = blockIdx.z * a.zb;
     const int z1 = min(a.nz, z0 + a.zb);
     const int zbn = z1 - z0;
-    const long long step = *a.step_base + koff;
 
     for (int e = tid; e < (int)(BD_MAX_MATERIALS * sizeof(MatConst<real>) / 4); e += NT)
         reinterpret_cast<unsigned*>(sK)[e] = reinterpret_cast<const unsigned*>(Kp)[e];
@@ -184,6 +183,12 @@ __global__ void __launch_bounds__(TX* TY / CPT) wv_tma_kernel(const WvArgs<real>
         mbar_fence_init();
     }
     __syncthreads();
+    // Programmatic dependent launch: with the attribute set by the host, the
+    // prologue above (material constants, barrier set-up) overlaps the tail of
+    // the previous step's grid; the fields and the step counter it wrote are
+    // read only after this wait (a no-op for an ordinary launch).
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    const long long step = *a.step_base + koff;
     if (tid == 0) {
         for (int q = 0; q < TMA_NP; ++q) issueP(q);
         for (int r = 0; r < TMA_NQ; ++r) issueQ(r);
@@ -232,6 +237,8 @@ __global__ void __launch_bounds__(TX* TY / CPT) wv_tma_kernel(const WvArgs<real>
     const MatConst<real> M0 = sK[0];
 
     for (int izg = z0; izg < z1; izg += ZU) {
+        // the last planes of this CTA: the next step's grid may start its prologue
+        if (izg + ZU >= z1) asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 #pragma unroll
     for (int u = 0; u < ZU; ++u) {
         const int iz = izg + u;
