@@ -15,6 +15,11 @@ dx = 0.1875 mm, heterogeneous c, one relaxation process, 20-cell sponge, 1 MHz
 
 --impl reference times the reference's own Westervelt kernels built for the
 host (oracle/_ref) on the same grid (its two-layer physics), all host cores.
+--impl reference-gpu times the reference's own CUDA kernels (W's step loop,
+G's DPRK_step one thread per bubble; oracle/_ref/libbdref_gpu.so) beside this
+library on the same problems (the comparison baseline of the speed-ups).
+The default line also carries the cfg3, cfg4, cfg5 and cfg2 summaries
+(--no-extra skips them).
 --gpus N under torchrun: N independent replicas (the solver does not shard).
 """
 import argparse
@@ -276,7 +281,6 @@ def run_westervelt(args, world, rank, local):
         line["cfg3"] = cfg3_summary(ctx)
         line["cfg5"] = cfg5_summary(ctx)
         line["gilmore"] = gilmore_summary(ctx, with_cpu=not args.no_cpu)
-        line["reference_gpu"] = reference_gpu_summary(ctx)
     if rank == 0:
         print(json.dumps(line), flush=True)
     ctx.close()
@@ -547,7 +551,7 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference", "reference-gpu"])
     ap.add_argument("--workload", default="westervelt",
                     choices=["westervelt", "step-kernel", "gilmore", "heat", "adjoint", "dft"])
     ap.add_argument("--bubbles", type=int, default=1 << 16, help="gilmore workload: bubbles")
@@ -562,6 +566,12 @@ def main():
     world, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, world, rank)
+    elif args.impl == "reference-gpu":
+        if rank == 0:
+            from bubbledynamics_gb300 import api
+            ctx = api.Context(0)
+            print(json.dumps({"impl": "reference-gpu", "comparison": reference_gpu_summary(ctx)}), flush=True)
+            ctx.close()
     elif args.workload == "step-kernel":
         if rank == 0:
             run_step_kernel(args)
