@@ -93,12 +93,18 @@ def have_reference_sources():
     return all(os.path.exists(os.path.join(REF_DIR, n)) for n in REF_FILES.values())
 
 
-def build_ref(force=False):
-    """Build oracle/_ref/libbdref.so; returns its path or None if no sources."""
-    src_dir = os.path.join(REF_OUT, "src")
+def extract_all():
+    """Extract the reference sections (when the reference tree is present)."""
     if have_reference_sources():
         extract_reference()
         extract_T_trajectory()
+
+
+def build_ref(force=False, extract=True):
+    """Build oracle/_ref/libbdref.so; returns its path or None if no sources."""
+    src_dir = os.path.join(REF_OUT, "src")
+    if extract:
+        extract_all()
     incs = [os.path.join(src_dir, "%s_kernels.inc" % k) for k in REF_FILES] + [os.path.join(src_dir, "T_traj.inc")]
     if not all(os.path.exists(p) for p in incs):
         return None
@@ -113,13 +119,13 @@ def build_ref(force=False):
 REF_GPU_SO = os.path.join(REF_OUT, "libbdref_gpu.so")
 
 
-def build_ref_gpu(force=False):
+def build_ref_gpu(force=False, extract=True):
     """Build oracle/_ref/libbdref_gpu.so: the reference's W and G kernel
     sections compiled by nvcc for sm_103a with the host loops of
     ref_gpu_harness.cu.  Returns its path, or None without the sections."""
     src_dir = os.path.join(REF_OUT, "src")
-    if have_reference_sources():
-        extract_reference()
+    if extract:
+        extract_all()
     incs = [os.path.join(src_dir, "%s_kernels.inc" % k) for k in ("W", "G")]
     if not all(os.path.exists(p) for p in incs):
         return None
