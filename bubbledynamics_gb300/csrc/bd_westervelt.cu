@@ -886,6 +886,14 @@ static void adj_launch_n(WvSession& S, const AdjArgs<real>& a, cudaStream_t st) 
         adj_point_kernel<real, NR, 1><<<(unsigned)((S.ncell + 255) / 256), 256, 0, st>>>(a, K);
     }
     BD_LAUNCHED(S.ctx);
+    if constexpr (sizeof(real) == 4) {
+        if (S.nx % 4 == 0) {
+            dim3 b(16, 8), g((S.nx / 4 + 15) / 16, (S.ny + 7) / 8, (S.nz + a.zb - 1) / a.zb);
+            adj_stencil4_kernel<<<g, b, 0, st>>>(a);
+            BD_LAUNCHED(S.ctx);
+            return;
+        }
+    }
     dim3 b(32, 8), g((S.nx + 31) / 32, (S.ny + 7) / 8, (S.nz + a.zb - 1) / a.zb);
     adj_stencil_kernel<real><<<g, b, 0, st>>>(a);
     BD_LAUNCHED(S.ctx);

@@ -401,4 +401,62 @@ __global__ void __launch_bounds__(256) adj_stencil_kernel(const AdjArgs<real> a)
     }
 }
 
+// The stencil pass on four consecutive x cells per thread (FP32, nx % 4 == 0):
+// every neighbour row comes as one 16-byte load — the row itself and the rows
+// 4 cells left and right for the x neighbours, six rows for y, one new plane
+// for z — instead of thirteen scalar loads per cell.
+__device__ __forceinline__ float4 ld4(const float* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
+__device__ __forceinline__ float4 add4(float4 a, float4 b) { return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
+
+__global__ void __launch_bounds__(128) adj_stencil4_kernel(const AdjArgs<float> a) {
+    const int x0 = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
+    const int iy = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x0 >= a.nx || iy >= a.ny) return;
+    const int z0 = blockIdx.z * a.zb;
+    const int z1 = min(a.nz, z0 + a.zb);
+    const long long col = (long long)iy * a.nx + x0;
+    const float* __restrict__ H = a.H;
+    float* __restrict__ lam = a.mu[1];
+    const long long nx = a.nx;
+    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+    auto row = [&](int z, int dy) -> float4 {
+        const int y = iy + dy;
+        if (z < 0 || z >= a.nz || y < 0 || y >= a.ny) return zero;
+        return ld4(H + (long long)z * a.plane + col + (long long)dy * nx);
+    };
+    float4 w[7];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) w[k] = row(z0 - 3 + k, 0);
+    for (int iz = z0; iz < z1; ++iz) {
+        w[6] = row(iz + 3, 0);
+        const float* P = H + (long long)iz * a.plane + col;
+        const float4 Lq = x0 >= 4 ? ld4(P - 4) : zero;
+        const float4 Rq = x0 + 4 < a.nx ? ld4(P + 4) : zero;
+        const float4 y1 = add4(row(iz, 1), row(iz, -1));
+        const float4 y2 = add4(row(iz, 2), row(iz, -2));
+        const float4 y3 = add4(row(iz, 3), row(iz, -3));
+        const long long i = (long long)iz * a.plane + col;
+        float4 l = *reinterpret_cast<const float4*>(lam + i);
+        // x values x0-4 .. x0+7
+        const float xs[12] = {Lq.x, Lq.y, Lq.z, Lq.w, w[3].x, w[3].y, w[3].z, w[3].w, Rq.x, Rq.y, Rq.z, Rq.w};
+        const float c[4] = {w[3].x, w[3].y, w[3].z, w[3].w};
+        const float ys1[4] = {y1.x, y1.y, y1.z, y1.w}, ys2[4] = {y2.x, y2.y, y2.z, y2.w}, ys3[4] = {y3.x, y3.y, y3.z, y3.w};
+        const float zp1[4] = {w[4].x, w[4].y, w[4].z, w[4].w}, zm1[4] = {w[2].x, w[2].y, w[2].z, w[2].w};
+        const float zp2[4] = {w[5].x, w[5].y, w[5].z, w[5].w}, zm2[4] = {w[1].x, w[1].y, w[1].z, w[1].w};
+        const float zp3[4] = {w[6].x, w[6].y, w[6].z, w[6].w}, zm3[4] = {w[0].x, w[0].y, w[0].z, w[0].w};
+        float out[4] = {l.x, l.y, l.z, l.w};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const float ax1 = xs[5 + k] + xs[3 + k], ax2 = xs[6 + k] + xs[2 + k], ax3 = xs[7 + k] + xs[1 + k];
+            const float h0 = c[k];
+            const float sxy = -980.f * h0 + 270.f * (ax1 + ys1[k]) - 27.f * (ax2 + ys2[k]) + 2.f * (ax3 + ys3[k]);
+            const float sz = -490.f * h0 + 270.f * (zp1[k] + zm1[k]) - 27.f * (zp2[k] + zm2[k]) + 2.f * (zp3[k] + zm3[k]);
+            out[k] = out[k] + a.kxy180 * sxy + a.kz180 * sz;
+        }
+        *reinterpret_cast<float4*>(lam + i) = make_float4(out[0], out[1], out[2], out[3]);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) w[k] = w[k + 1];
+    }
+}
+
 }  // namespace bd
