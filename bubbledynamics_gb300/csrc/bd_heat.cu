@@ -127,6 +127,81 @@ __global__ void heat_step_kernel(const HeatArgs<real> a, int koff) {
     }
 }
 
+// FP32 step on four consecutive x cells per thread (nx % 4 == 0): theta, its
+// neighbour rows and the dose pairs move as 16-byte vectors; the source Q,
+// shifted by any whole number of cells, is read per cell.  Face cells keep
+// their value (they are written back unchanged), like the scalar kernel.
+__global__ void __launch_bounds__(128) heat_step4_kernel(const HeatArgs<float> a, int koff) {
+    const int x0 = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
+    const int iy = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x0 >= a.nx || iy < 1 || iy >= a.ny - 1) return;
+    const long long step = *a.step_base + koff;
+    const int2 sh = a.shifts[step];
+    const int iya = iy - sh.y;                                   // T:61-62
+    const bool qrow = iya >= 0 && iya < a.ny;
+    const long long col = (long long)iy * a.nx + x0;
+    const int z0 = max(1, blockIdx.z * a.zb);
+    const int z1 = min(a.nz - 1, blockIdx.z * a.zb + a.zb);
+    if (z0 >= z1) return;
+    const long long P = a.plane, NX = a.nx;
+    auto ld4 = [](const float* p) { return __ldg(reinterpret_cast<const float4*>(p)); };
+    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 tm = ld4(a.Tin + (long long)(z0 - 1) * P + col);
+    float4 tc = ld4(a.Tin + (long long)z0 * P + col);
+    bool upd[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) upd[k] = x0 + k >= 1 && x0 + k < a.nx - 1;
+    for (int iz = z0; iz < z1; ++iz) {
+        const long long i = (long long)iz * P + col;
+        const float4 tp = ld4(a.Tin + i + P);
+        const float4 L = x0 >= 4 ? ld4(a.Tin + i - 4) : zero;
+        const float4 R = x0 + 4 < a.nx ? ld4(a.Tin + i + 4) : zero;
+        const float4 yu = ld4(a.Tin + i + NX), yd = ld4(a.Tin + i - NX);
+        float q[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {                             // T:76-77
+            const int ixa = x0 + k - sh.x;
+            q[k] = (qrow && ixa >= 0 && ixa < a.nx) ? __ldg(a.Q + (long long)iz * P + (long long)iya * NX + ixa) : 0.f;
+        }
+        float4* dp = reinterpret_cast<float4*>(a.TDf + i);
+        float4 d01 = dp[0], d23 = dp[1];
+        int mats[4];
+        if (a.matmap) {
+            const uchar4 mm = *reinterpret_cast<const uchar4*>(a.matmap + i);
+            mats[0] = mm.x; mats[1] = mm.y; mats[2] = mm.z; mats[3] = mm.w;
+        } else {
+            const int m = a.plane_mat ? __ldg(a.plane_mat + iz) : 0;
+            mats[0] = mats[1] = mats[2] = mats[3] = m;
+        }
+        const float cv[4] = {tc.x, tc.y, tc.z, tc.w};
+        const float xl[4] = {L.w, tc.x, tc.y, tc.z}, xr[4] = {tc.y, tc.z, tc.w, R.x};
+        const float su[4] = {yu.x, yu.y, yu.z, yu.w}, sd[4] = {yd.x, yd.y, yd.z, yd.w};
+        const float zu[4] = {tp.x, tp.y, tp.z, tp.w}, zd[4] = {tm.x, tm.y, tm.z, tm.w};
+        float dh[4] = {d01.x, d01.z, d23.x, d23.z}, dl[4] = {d01.y, d01.w, d23.y, d23.w};
+        float tn[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const HeatMat<float>& M = a.mat[mats[k]];
+            const float sxy = xl[k] + xr[k] + su[k] + sd[k];
+            // T:85-87 (plus the Pennes term -w dt (T - T_art), zero in the reference)
+            const float t = cv[k] * M.a0 + M.kxy * sxy + M.kz * (zu[k] + zd[k]) + M.qc * q[k] + M.wTa;
+            tn[k] = upd[k] ? t : cv[k];
+            if (upd[k]) {
+                const float x = t + a.T_refm43;                   // T_C - 43
+                const float inc = exp2f(x < 0.0f ? 2.0f * x : x) * a.dt;
+                const float2 r = df_add(make_float2(dh[k], dl[k]), inc);
+                dh[k] = r.x;
+                dl[k] = r.y;
+            }
+        }
+        *reinterpret_cast<float4*>(a.Tout + i) = make_float4(tn[0], tn[1], tn[2], tn[3]);
+        dp[0] = make_float4(dh[0], dl[0], dh[1], dl[1]);
+        dp[1] = make_float4(dh[2], dl[2], dh[3], dl[3]);
+        tm = tc;
+        tc = tp;
+    }
+}
+
 __global__ void heat_advance_kernel(long long* step_base, int n) {
     if (threadIdx.x == 0 && blockIdx.x == 0) *step_base += n;
 }
@@ -329,6 +404,7 @@ bd_status bd_spiral_heat_run(bd_context* ctx, const bd_thermal* th, const double
         cudaStream_t s = ctx->stream;
         const int zb = 32;
         dim3 block(32, 8), grid((nx + 31) / 32, (ny + 7) / 8, (nz + zb - 1) / zb);
+        dim3 block4(16, 8), grid4((nx / 4 + 15) / 16, (ny + 7) / 8, (nz + zb - 1) / zb);
         // snapshot schedule: after the listed legs (T:412-563)
         std::vector<std::pair<int64_t, int>> snaps;
         for (int k = 0; k < out->n_snap; ++k) {
@@ -401,7 +477,8 @@ bd_status bd_spiral_heat_run(bd_context* ctx, const bd_thermal* th, const double
                     } else {
                         HeatArgs<float> a = margs.first;
                         fill(a, a_to_b, 0.0f);
-                        heat_step_kernel<float><<<grid, block, 0, s>>>(a, k);
+                        if (nx % 4 == 0) heat_step4_kernel<<<grid4, block4, 0, s>>>(a, k);
+                        else heat_step_kernel<float><<<grid, block, 0, s>>>(a, k);
                     }
                     BD_LAUNCHED(ctx);
                 }
