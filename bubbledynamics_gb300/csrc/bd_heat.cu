@@ -402,7 +402,15 @@ bd_status bd_spiral_heat_run(bd_context* ctx, const bd_thermal* th, const double
         }
         BD_CUDA(cudaMemset(sb.p, 0, 64));
         cudaStream_t s = ctx->stream;
-        const int zb = 32;
+        const bool vec4 = !f64 && nx % 4 == 0;
+        int zb = 32;
+        if (vec4) {
+            // four-cell kernel: z-chunk fitted to whole waves of its resident CTAs
+            static int per_sm = 0;
+            if (!per_sm) BD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, heat_step4_kernel, 128, 0));
+            const long long tiles = (long long)((nx / 4 + 15) / 16) * ((ny + 7) / 8);
+            zb = wave_fitted_zb(tiles, nz, (long long)ctx->sm_count * std::max(per_sm, 1), 0.9);
+        }
         dim3 block(32, 8), grid((nx + 31) / 32, (ny + 7) / 8, (nz + zb - 1) / zb);
         dim3 block4(16, 8), grid4((nx / 4 + 15) / 16, (ny + 7) / 8, (nz + zb - 1) / zb);
         // snapshot schedule: after the listed legs (T:412-563)
@@ -477,7 +485,7 @@ bd_status bd_spiral_heat_run(bd_context* ctx, const bd_thermal* th, const double
                     } else {
                         HeatArgs<float> a = margs.first;
                         fill(a, a_to_b, 0.0f);
-                        if (nx % 4 == 0) heat_step4_kernel<<<grid4, block4, 0, s>>>(a, k);
+                        if (vec4) heat_step4_kernel<<<grid4, block4, 0, s>>>(a, k);
                         else heat_step_kernel<float><<<grid, block, 0, s>>>(a, k);
                     }
                     BD_LAUNCHED(ctx);

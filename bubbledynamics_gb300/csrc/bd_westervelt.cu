@@ -216,22 +216,6 @@ static void build_maps(WvSession& S, int tx, int ty) {
     S.maps_ty = ty;
 }
 
-// z-chunk for which tiles * ceil(nz / zb) CTAs fill whole waves of `slots`
-// resident CTAs (at least 97 % of the last wave busy), the largest such
-// chunk of at least 8 planes; 16 if none qualifies.
-static int wave_fitted_zb(long long tiles, int nz, long long slots) {
-    for (int w = 1; w <= 16; ++w) {
-        const long long chunks = (w * slots + tiles - 1) / tiles;
-        if (chunks > nz) break;
-        const int zb = (int)((nz + chunks - 1) / chunks);
-        if (zb < 8) break;
-        const long long n = tiles * ((nz + zb - 1) / zb);
-        const long long cap = ((n + slots - 1) / slots) * slots;
-        if ((double)n >= 0.97 * (double)cap) return zb;
-    }
-    return 16;
-}
-
 template <class real, int TX, int TY, int CPT, int NREL, int ZU, int FL = -1>
 static void launch_tma_k(WvSession& S, const WvArgs<real>& a0, const TmaMaps& maps, int koff, cudaStream_t st) {
     using L = TmaLayout<real, TX, TY, (NREL >= 0 ? NREL : BD_MAX_RELAX)>;
