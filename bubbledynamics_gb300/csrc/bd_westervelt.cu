@@ -872,8 +872,14 @@ static void adj_launch_n(WvSession& S, const AdjArgs<real>& a, cudaStream_t st) 
     BD_LAUNCHED(S.ctx);
     if constexpr (sizeof(real) == 4) {
         if (S.nx % 4 == 0) {
-            dim3 b(16, 8), g((S.nx / 4 + 15) / 16, (S.ny + 7) / 8, (S.nz + a.zb - 1) / a.zb);
-            adj_stencil4_kernel<<<g, b, 0, st>>>(a);
+            // z-chunk fitted to whole waves of the four-cell kernel's resident CTAs
+            static int per_sm = 0;
+            if (!per_sm) BD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, adj_stencil4_kernel, 128, 0));
+            AdjArgs<real> a4 = a;
+            const long long tiles = (long long)((S.nx / 4 + 15) / 16) * ((S.ny + 7) / 8);
+            a4.zb = wave_fitted_zb(tiles, S.nz, (long long)S.ctx->sm_count * std::max(per_sm, 1), 0.9);
+            dim3 b(16, 8), g((S.nx / 4 + 15) / 16, (S.ny + 7) / 8, (S.nz + a4.zb - 1) / a4.zb);
+            adj_stencil4_kernel<<<g, b, 0, st>>>(a4);
             BD_LAUNCHED(S.ctx);
             return;
         }
