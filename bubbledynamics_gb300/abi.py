@@ -158,6 +158,7 @@ class Thermal(C.Structure):
         ("n_materials", i32), ("dose_init", i32),
         ("mat", ThermalMaterial * BD_MAX_MATERIALS),
         ("plane_material", vp), ("material_map", vp),
+        ("T_start", vp), ("dose_start", vp),
     ]
 
 

@@ -363,8 +363,9 @@ bd_status bd_spiral_heat_run(bd_context* ctx, const bd_thermal* th, const double
         std::vector<double> T0(n), TD0(n);
         for (long long i = 0; i < n; ++i) {
             const bd_thermal_material& mt = th->mat[mat_of(i)];
-            T0[i] = mt.T_init;
-            TD0[i] = th->dose_init ? std::pow(4.0, mt.T_init - 273.15 - 43.0) * th->dt : 0.0;   // T:246, T:252
+            T0[i] = th->T_start ? th->T_start[i] : mt.T_init;
+            TD0[i] = th->dose_start ? th->dose_start[i]
+                                    : (th->dose_init ? std::pow(4.0, mt.T_init - 273.15 - 43.0) * th->dt : 0.0);   // T:246, T:252
         }
         const size_t esz = f64 ? 8 : 4;
         PoolBuf Ta, Tb, Qd, TDd, pm, mm, shd, sb;

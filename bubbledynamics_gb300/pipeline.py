@@ -49,6 +49,46 @@ def cfg3_run(ctx, acoustic=None, n_spots=None, steps_per_spot=None, thermal_prec
             "T": h["T"], "dose": h["dose"], "heat_ms": h["elapsed_ms"], "heat_steps": h["steps_done"]}
 
 
+def steered_spots_run(ctx, acoustic, n_spots=None, steps_per_spot=None, thermal_precision=abi.BD_F32,
+                      keep_q=False):
+    """The spiral of cfg3 with the field re-solved for every spot (instead of
+    translating one Q, T:61-77): the array source of `acoustic` (cfg3_array) is
+    steered electronically to each spot, the Westervelt solve gives that
+    spot's Q, and the heat run continues from the previous spot's temperature
+    and dose with the source in place.  Returns the final T and dose, the
+    focal peak position per spot and the device times."""
+    from . import presets as P
+    g = acoustic.grid
+    theta, phi = acoustic.meta["elements"]
+    F = acoustic.source.focal_length
+    f = acoustic.source.freq[0]
+    th0 = P.cfg3_thermal(acoustic, n_spots=n_spots, steps_per_spot=steps_per_spot, precision=thermal_precision)
+    sx, sy, steps = th0._keep["spot_sx"], th0._keep["spot_sy"], th0._keep["spot_steps"]
+    T, dose = th0.initial_fields()
+    amps = acoustic.array("element_amp")
+    elem = acoustic.array("element_of_cell")
+    peaks, qs, ac_ms, heat_ms = [], [], 0.0, 0.0
+    izf = acoustic.source.plane_iz + int(round(F / g.dz))
+    for k in range(len(sx)):
+        q = acoustic.copy()
+        q.set_elements(elem, P.steering_phases(theta, phi, F, (sx[k] * g.dx, sy[k] * g.dx, 0.0), f, 1500.0), amps)
+        r = ctx.westervelt(q, want=("energy", "peak"))
+        ac_ms += r["elapsed_ms"]
+        pk = r["peak"][izf]
+        peaks.append(np.unravel_index(int(np.argmax(pk)), pk.shape))
+        Q = heat_source_from_energy(q, r["energy"], q.meta["window_s"])
+        if keep_q:
+            qs.append(Q)
+        th = P.cfg3_thermal(acoustic, n_spots=1, steps_per_spot=int(steps[k]), precision=thermal_precision)
+        th.set_spots([0], [0], [int(steps[k])])
+        th.set_start(T, dose)
+        h = ctx.heat(th.thermal, Q, th.traj)
+        heat_ms += h["elapsed_ms"]
+        T, dose = h["T"], h["dose"]
+    return {"T": T, "dose": dose, "focal_peaks": peaks, "spots": list(zip(sx.tolist(), sy.tolist())),
+            "steps": steps.tolist(), "Q": qs, "acoustic_ms": ac_ms, "heat_ms": heat_ms}
+
+
 def bubbles_from_dft(prob, dft_re, dft_im, n, seed=5, radius=2e-3, length=5e-3, R0_range=(0.5e-6, 5e-6)):
     """n bubbles at seeded random points of the focal region (a cylinder of
     `radius` and +-`length` around the focus), each driven by the field at its

@@ -383,6 +383,41 @@ def fibonacci_cap(n, alpha):
     return theta, phi
 
 
+def assign_cap_elements(prob, n_elements, F, aperture):
+    """Make prob's source a cap-shaped array of n_elements (Fibonacci points of
+    the cap of focal length F and planar aperture radius `aperture`): every
+    source-plane cell inside the aperture belongs to the element whose
+    projected centre F tan(theta) (cos phi, sin phi) is nearest.  Phases 0,
+    amplitudes 1.  Returns the element angles (theta, phi)."""
+    g = prob.grid
+    theta, phi = fibonacci_cap(n_elements, math.atan(aperture / F))
+    ex = F * np.tan(theta) * np.cos(phi)
+    ey = F * np.tan(theta) * np.sin(phi)
+    xs = g.x0 + g.dx * np.arange(g.nx)
+    ys = g.y0 + g.dx * np.arange(g.ny)
+    X, Y = np.meshgrid(xs, ys, indexing="xy")
+    d2 = (X[..., None] - ex) ** 2 + (Y[..., None] - ey) ** 2
+    elem = np.argmin(d2, axis=-1).astype(np.int32)
+    elem[np.hypot(X, Y) > aperture] = -1
+    prob.source.kind = abi.BD_SRC_ARRAY
+    prob.set_elements(elem.reshape(-1), np.zeros(n_elements), np.ones(n_elements))
+    prob.meta["elements"] = (theta, phi)
+    return theta, phi
+
+
+def steering_phases(theta, phi, F, offset, f, c0):
+    """Element phases that move the focus of a cap array (focal length F,
+    element angles theta / phi) by `offset` = (dx, dy, dz) [m] from its
+    geometric focus: each element fires earlier by its extra path to the new
+    point, (|r_e - r_spot| - F) / c0, i.e. phase 2 pi f times that."""
+    ex = F * np.sin(theta) * np.cos(phi)
+    ey = F * np.sin(theta) * np.sin(phi)
+    ez = -F * np.cos(theta)                     # the cap lies below the focus
+    dxs, dys, dzs = offset
+    dist = np.sqrt((ex - dxs) ** 2 + (ey - dys) ** 2 + (ez - dzs) ** 2)
+    return 2.0 * math.pi * f * (dist - F) / c0
+
+
 def slab_materials(f):
     """Water / fat / liver (c, rho, beta, delta, relaxation)."""
     water = _material(1500.0, 1000.0, 3.5, water_delta(f, 1500.0))
@@ -450,18 +485,9 @@ def focal_array_problem(nx, ny, nz, dx, n_elements, n_steps, window, F, aperture
         zi = sponge + frac * depth + jit.reshape(1, ny, nx)
         mm[z >= zi] = k + 1
     prob.set_material_map(mm)
-    # elements: nearest projected cap point for every plane cell inside the aperture
-    theta, phi = fibonacci_cap(n_elements, math.atan(aperture / F))
-    ex = F * np.tan(theta) * np.cos(phi)
-    ey = F * np.tan(theta) * np.sin(phi)
-    xs = g.x0 + dx * np.arange(nx)
-    ys = g.y0 + dx * np.arange(ny)
-    X, Y = np.meshgrid(xs, ys, indexing="xy")
-    d2 = (X[..., None] - ex) ** 2 + (Y[..., None] - ey) ** 2
-    elem = np.argmin(d2, axis=-1).astype(np.int32)
-    elem[np.hypot(X, Y) > aperture] = -1
+    theta, phi = assign_cap_elements(prob, n_elements, F, aperture)
     phase = rng.uniform(0.0, 2.0 * math.pi, n_elements)
-    prob.set_elements(elem.reshape(-1), phase, np.ones(n_elements))
+    prob.set_elements(prob.array("element_of_cell"), phase, np.ones(n_elements))
     loss = abi.FocalLoss()
     loss.focus_ix, loss.focus_iy = nx // 2, ny // 2
     loss.focus_iz = min(nz - sponge - 1, sponge + int(round(F / dx)))
@@ -524,8 +550,19 @@ class ThermalProblem:
         self.traj.n_spots = sx.size
         self.traj.spot_sx, self.traj.spot_sy, self.traj.spot_steps = abi.ptr(sx), abi.ptr(sy), abi.ptr(st)
 
+    def set_start(self, T, dose):
+        """Start the next run from these fields (a run continuing an earlier one)."""
+        T = np.ascontiguousarray(T, dtype=np.float64)
+        dose = np.ascontiguousarray(dose, dtype=np.float64)
+        self._keep.update(T_start=T, dose_start=dose)
+        self.thermal.T_start, self.thermal.dose_start = abi.ptr(T), abi.ptr(dose)
+
     def initial_fields(self):
-        """Initial T and dose as T:232-257 sets them (dose_init = 1)."""
+        """Initial T and dose as T:232-257 sets them (dose_init = 1), or the
+        start fields of set_start."""
+        if self._keep.get("T_start") is not None:
+            return (self._keep["T_start"].reshape(self.shape).copy(),
+                    self._keep["dose_start"].reshape(self.shape).copy())
         t = self.thermal
         pm = self._keep.get("plane_material")
         T = np.zeros(self.shape)
@@ -696,6 +733,17 @@ def cfg3_acoustic(nx=None, ny=None, nz=None, n_steps=None, precision=abi.BD_F32)
                              meta={"f": k["f"], "alpha0": a0, "fit_error": err, "window_s": n_win * g.dt})
     iz_liver = sponge + int(round(k["water_mm"] * 1e-3 * scale / dx))
     prob.set_plane_material([0 if iz < iz_liver else 1 for iz in range(nz)])
+    return prob
+
+
+def cfg3_array(n_elements=256, **kw):
+    """cfg3's acoustic problem with the bowl split into a cap-shaped array of
+    n_elements, for electronic steering of the focus (steering_phases)."""
+    prob = cfg3_acoustic(**kw)
+    F = prob.source.focal_length
+    aperture = F * math.tan(prob.source.alpha)
+    assign_cap_elements(prob, n_elements, F, aperture)
+    prob.name = "cfg3_array"
     return prob
 
 

@@ -275,6 +275,9 @@ typedef struct bd_thermal {
     bd_thermal_material mat[BD_MAX_MATERIALS];
     const int32_t* plane_material;  /* nz entries (T:84 split by z) */
     const uint8_t* material_map;    /* optional nx*ny*nz */
+    const double* T_start;          /* optional nx*ny*nz initial temperature [K] (NULL: mat[].T_init) */
+    const double* dose_start;       /* optional nx*ny*nz initial dose [s] (NULL: dose_init rule);
+                                       with both, a run continues where an earlier one ended */
 } bd_thermal;
 
 typedef enum bd_trajectory_kind {
