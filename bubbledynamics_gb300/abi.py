@@ -58,6 +58,8 @@ BD_BUBBLE_NONFINITE = 3
 
 BD_SCHEDULE_PERSISTENT = 0
 BD_SCHEDULE_STATIC = 1
+BD_SEARCH_LINEAR = 0
+BD_SEARCH_BISECT = 1
 
 BD_SLICE_XZ = 0
 BD_SLICE_XY = 1

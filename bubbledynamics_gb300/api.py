@@ -74,6 +74,8 @@ def load(path=None):
     _sig(L, "bd_gilmore_run_device", [P, P, C.c_int64, P, P, P, P])
     _sig(L, "bd_gilmore_threshold", [P, P, P, C.c_int64, P, C.c_int64, C.c_int32, C.c_int64, P,
                                      C.POINTER(C.c_double)])
+    _sig(L, "bd_gilmore_threshold_search", [P, P, P, C.c_int64, P, C.c_int64, C.c_int32, C.c_int64, C.c_int32, P,
+                                            C.POINTER(C.c_double)])
     _sig(L, "bd_heat_run_device_noalloc", [P, P, P, P, P, P, C.c_int64, P])
     _sig(L, "bd_westervelt_adjoint", [P, P, P, P, P, P, C.POINTER(C.c_double), P, P, P])
     _sig(L, "bd_write_q_bin", [C.c_char_p, P, C.c_int32, C.c_int32, C.c_int32, C.c_int32])
@@ -298,14 +300,16 @@ class Context:
                                     _ptr(res), C.byref(ms)))
         return res, ms.value
 
-    def gilmore_threshold(self, medium, fr_combo, R0, ref_arith=1, max_steps=0):
+    def gilmore_threshold(self, medium, fr_combo, R0, ref_arith=1, max_steps=0, search=abi.BD_SEARCH_LINEAR):
+        """G's threshold search per (combination, R0); search=BD_SEARCH_BISECT
+        bisects the last 0.1 MPa bracket instead of G's 10 kPa / 1 kPa scan."""
         fr = np.ascontiguousarray(fr_combo, dtype=np.float64).reshape(-1)
         R0 = np.ascontiguousarray(R0, dtype=np.float64)
         nc = fr.size // 3
         out = np.zeros(nc * R0.size, np.float64)
         ms = C.c_double(0)
-        check(self.L.bd_gilmore_threshold(self.h, C.byref(medium), _ptr(fr), nc, _ptr(R0), R0.size, ref_arith,
-                                          max_steps, _ptr(out), C.byref(ms)))
+        check(self.L.bd_gilmore_threshold_search(self.h, C.byref(medium), _ptr(fr), nc, _ptr(R0), R0.size, ref_arith,
+                                                 max_steps, search, _ptr(out), C.byref(ms)))
         return out.reshape(nc, R0.size), ms.value
 
 

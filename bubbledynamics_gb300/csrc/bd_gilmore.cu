@@ -543,9 +543,11 @@ __global__ void __launch_bounds__(128) gilmore_threshold_kernel(const double* __
                                                                 const double* __restrict__ R0s, long long n_R0,
                                                                 const GilK g, const OdeK o, double* __restrict__ out,
                                                                 unsigned long long* __restrict__ counter,
-                                                                unsigned long long* __restrict__ capped) {
+                                                                unsigned long long* __restrict__ capped,
+                                                                int bisect) {
     const int max_rej_per_step = 200;
     const long long N = n_combo * n_R0;
+    int ilo = 0, ihi = 0, imid = 0;   // bisection (stage 2) on A = A5 - 0.1 MPa + i kPa
     Lane L;
     Tones d;
     long long item = -1;
@@ -581,7 +583,19 @@ __global__ void __launch_bounds__(128) gilmore_threshold_kernel(const double* __
                     else {
                         if (!th5 && A5 == 1e7) result = A5;                              // G:383-387
                         A4 = A5;
-                        stage = 4;
+                        if (bisect) { stage = 2; ilo = 0; ihi = 100; }
+                        else stage = 4;
+                    }
+                } else if (stage == 2) {
+                    // bisection between A5 - 0.1 MPa (below the threshold) and A5 (reached)
+                    if (th5 && ihi - ilo > 1) {
+                        imid = (ilo + ihi) / 2;
+                        L.h = 1e-13;
+                        A = (A5 - 1e5) + imid * 1e3;
+                        start = true;
+                    } else {
+                        if (th5) result = (A5 - 1e5) + ihi * 1e3;
+                        finish = true;
                     }
                 } else if (stage == 4) {
                     if (th5 && th4) { L.h = 1e-13; A4 = A4 - 1e4; A = A4; start = true; }   // G:391-396
@@ -628,6 +642,7 @@ __global__ void __launch_bounds__(128) gilmore_threshold_kernel(const double* __
         if (ended) {
             running = false;
             if (stage == 5) th5 = hit;
+            else if (stage == 2) { if (hit) ihi = imid; else ilo = imid; }
             else if (stage == 4) { th4 = hit; if (!th4) A4 = A4 + 1e4; }                  // G:401-405
             else if (stage == 3) { th3 = hit; if (!th3) result = A3 + 1e3; }               // G:421-424
         }
@@ -742,9 +757,18 @@ bd_status bd_gilmore_run_device(bd_context* ctx, const bd_gilmore_medium* medium
 bd_status bd_gilmore_threshold(bd_context* ctx, const bd_gilmore_medium* medium, const double* fr_combo, int64_t n_combo,
                                const double* R0, int64_t n_R0, int32_t ref_arith, int64_t max_steps, double* results,
                                double* elapsed_ms) {
+    return bd_gilmore_threshold_search(ctx, medium, fr_combo, n_combo, R0, n_R0, ref_arith, max_steps, BD_SEARCH_LINEAR,
+                                       results, elapsed_ms);
+}
+
+bd_status bd_gilmore_threshold_search(bd_context* ctx, const bd_gilmore_medium* medium, const double* fr_combo,
+                                      int64_t n_combo, const double* R0, int64_t n_R0, int32_t ref_arith,
+                                      int64_t max_steps, int32_t search, double* results, double* elapsed_ms) {
     return guard([&] {
         ctx_check(ctx);
         check_medium(medium);
+        if (search != BD_SEARCH_LINEAR && search != BD_SEARCH_BISECT)
+            fail(BD_ERR_INVALID_ARG, "search must be BD_SEARCH_LINEAR or BD_SEARCH_BISECT");
         if (n_combo < 0 || n_R0 < 0 || ((n_combo * n_R0) > 0 && (!fr_combo || !R0 || !results)))
             fail(BD_ERR_INVALID_ARG, "bad threshold arrays");
         const long long N = n_combo * n_R0;
@@ -771,7 +795,7 @@ bd_status bd_gilmore_threshold(bd_context* ctx, const bd_gilmore_medium* medium,
         const int grid = persistent_grid(ctx, (const void*)gilmore_threshold_kernel);
         unsigned long long* cnt = dc.as<unsigned long long>();
         gilmore_threshold_kernel<<<grid, 128, 0, st>>>(dfr.as<double>(), n_combo, dR0.as<double>(), n_R0, g, o,
-                                                       dout.as<double>(), cnt, cnt + 1);
+                                                       dout.as<double>(), cnt, cnt + 1, search == BD_SEARCH_BISECT);
         BD_LAUNCHED(ctx);
         BD_CUDA(cudaEventRecord(ctx->ev1, st));
         BD_CUDA(cudaMemcpyAsync(results, dout.p, N * 8, cudaMemcpyDeviceToHost, st));

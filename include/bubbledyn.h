@@ -444,6 +444,22 @@ bd_status bd_gilmore_threshold(bd_context* ctx, const bd_gilmore_medium* medium,
                                const double* R0, int64_t n_R0, int32_t ref_arith,
                                int64_t max_steps, double* results, double* elapsed_ms);
 
+typedef enum bd_search {
+    BD_SEARCH_LINEAR = 0,       /* G's scan: 0.1 MPa up, then 10 kPa and 1 kPa down (G:367-425) */
+    BD_SEARCH_BISECT = 1        /* 0.1 MPa up as G, then bisection in 1 kPa units inside the last
+                                   0.1 MPa bracket: 7 integrations instead of up to 20; equal to the
+                                   linear scan wherever cavitation is monotonic in the amplitude
+                                   inside that bracket */
+} bd_search;
+
+/* bd_gilmore_threshold with the search chosen (bd_search); BD_SEARCH_LINEAR is
+ * bd_gilmore_threshold itself. */
+bd_status bd_gilmore_threshold_search(bd_context* ctx, const bd_gilmore_medium* medium,
+                                      const double* fr_combo, int64_t n_combo,
+                                      const double* R0, int64_t n_R0, int32_t ref_arith,
+                                      int64_t max_steps, int32_t search, double* results,
+                                      double* elapsed_ms);
+
 /* ------------------------------------------------------------------------- */
 /* The reference programs' files (host only)                                  */
 /* ------------------------------------------------------------------------- */

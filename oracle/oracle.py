@@ -39,6 +39,8 @@ class Oracle:
         L.bdo_gilmore_run.restype = C.c_int
         L.bdo_gilmore_threshold.argtypes = [P, P, C.c_int64, P, C.c_int64, C.c_int64, P]
         L.bdo_gilmore_threshold.restype = C.c_int
+        L.bdo_gilmore_threshold_bisect.argtypes = [P, P, C.c_int64, P, C.c_int64, C.c_int64, P]
+        L.bdo_gilmore_threshold_bisect.restype = C.c_int
         L.bdo_gilmore_forward_combo.argtypes = [P, C.c_int64, P, P, P, C.c_double, C.c_double, C.c_int64,
                                                  C.c_int32, P, P, P]
         L.bdo_gilmore_forward_combo.restype = C.c_int
@@ -152,12 +154,13 @@ class Oracle:
                                            1 if stop_at_threshold else 0, _ptr(state), _ptr(counts), _ptr(thr))
         return state, counts, thr
 
-    def gilmore_threshold(self, medium, fr_combo, R0, max_steps=0):
+    def gilmore_threshold(self, medium, fr_combo, R0, max_steps=0, bisect=False):
         fr = np.ascontiguousarray(fr_combo, dtype=np.float64).reshape(-1)
         R0 = np.ascontiguousarray(R0, dtype=np.float64)
         nc = fr.size // 3
         out = np.zeros(nc * R0.size, np.float64)
-        self.lib.bdo_gilmore_threshold(C.byref(medium), _ptr(fr), nc, _ptr(R0), R0.size, max_steps, _ptr(out))
+        fn = self.lib.bdo_gilmore_threshold_bisect if bisect else self.lib.bdo_gilmore_threshold
+        fn(C.byref(medium), _ptr(fr), nc, _ptr(R0), R0.size, max_steps, _ptr(out))
         return out.reshape(nc, R0.size)
 
     def gilmore_combos(self, n_fr=55, f_min=0.02e6, f_max=5.0e6):

@@ -72,6 +72,20 @@ def test_threshold_search_matches_oracle_with_step_cap(ctx, oracle):
         np.testing.assert_array_equal(A, exp)
 
 
+def test_threshold_bisection_mode(ctx, oracle, lib):
+    """BD_SEARCH_BISECT runs through the same kernel and agrees with the
+    oracle's bisection search under the same step cap; an unknown search mode
+    is refused before any launch."""
+    g = np.load(golden_path("G_threshold.npz"))
+    med = presets.ref_G_medium()
+    exp = oracle.gilmore_threshold(med, g["combos"], g["R0"], max_steps=300, bisect=True)
+    A, ms = ctx.gilmore_threshold(med, g["combos"], g["R0"], max_steps=300, search=abi.BD_SEARCH_BISECT)
+    print("capped threshold, bisection: %.0f ms" % ms)
+    np.testing.assert_array_equal(A, exp)
+    with pytest.raises(api.BDError):
+        ctx.gilmore_threshold(med, g["combos"], g["R0"], max_steps=300, search=7)
+
+
 def test_every_bubble_processed_once(ctx, oracle):
     """3000 bubbles with uneven step counts through the work-stealing queue:
     every result row is written, and a sample matches the oracle row by row."""

@@ -77,6 +77,16 @@ def test_gilmore_threshold_matches_reference_fixture(oracle):
     np.testing.assert_array_equal(A, g["A"])
 
 
+def test_gilmore_threshold_bisection_matches_reference_fixture(oracle):
+    """The opt-in bisection search (stages 2-3 of G:391-426 replaced by
+    bisection on the 1 kPa grid inside the last 0.1 MPa bracket) lands on the
+    amplitudes of the reference's linear scan for a combination whose
+    threshold response is monotone."""
+    g = np.load(golden_path("G_threshold.npz"))
+    A = oracle.gilmore_threshold(presets.ref_G_medium(), g["combos"][3:], g["R0"], bisect=True)
+    np.testing.assert_array_equal(A, g["A"][3:])
+
+
 def test_gilmore_forward_matches_reference_fixture(oracle):
     """G's DPRK_step loop (G:212-318, G:378) for moderate drives to endT and one
     strong drive stopped at R' <= -C_inf: bit-identical."""
