@@ -532,7 +532,7 @@ def run_step_kernel(args):
     The case the ncu captures of the step kernel run."""
     from bubbledynamics_gb300 import api
     ctx = api.Context(0)
-    variants = [args.tile_variant] if args.tile_variant >= 0 else list(range(8, 19))
+    variants = [args.tile_variant] if args.tile_variant >= 0 else list(range(8, 24))
     out = {}
     for v in variants:
         prob = cfg1_problem()

@@ -123,17 +123,21 @@ void after_launch(bd_context* ctx, const char* file, int line);
 void ctx_check(bd_context* ctx);
 // z-chunk for which tiles * ceil(nz / zb) CTAs fill whole waves of `slots`
 // resident CTAs (at least `fill` of the last wave busy), the largest such
-// chunk of at least 8 planes; 16 if none qualifies.
+// chunk of at least 8 planes with the chunk count rounded up to cover w waves;
+// failing that, the chunk count rounded down (just under w waves); 16 if
+// neither qualifies.
 inline int wave_fitted_zb(long long tiles, int nz, long long slots, double fill = 0.97) {
-    for (int w = 1; w <= 16; ++w) {
-        const long long chunks = (w * slots + tiles - 1) / tiles;
-        if (chunks > nz) break;
-        const int zb = (int)((nz + chunks - 1) / chunks);
-        if (zb < 8) break;
-        const long long n = tiles * ((nz + zb - 1) / zb);
-        const long long cap = ((n + slots - 1) / slots) * slots;
-        if ((double)n >= fill * (double)cap) return zb;
-    }
+    for (int down = 0; down < 2; ++down)
+        for (int w = 1; w <= 16; ++w) {
+            const long long chunks = down ? (w * slots) / tiles : (w * slots + tiles - 1) / tiles;
+            if (chunks > nz) break;
+            if (chunks < 1) continue;
+            const int zb = (int)((nz + chunks - 1) / chunks);
+            if (zb < 8) break;
+            const long long n = tiles * ((nz + zb - 1) / zb);
+            const long long cap = ((n + slots - 1) / slots) * slots;
+            if ((double)n >= fill * (double)cap) return zb;
+        }
     return 16;
 }
 

@@ -28,19 +28,25 @@
 #include "wv_kernels.cuh"
 #include "wv_tma.cuh"
 #include "wv_adjoint.cuh"
+#include "wv_tma_pair.h"
 
 namespace bd {
 
-// Kernel variants: 0-7 plain (read-only-cache neighbours), 8-15 TMA-pipelined
-// (need a row pitch that is a multiple of 16 bytes).
-struct Variant { int tx, ty, zb, tma, cpt, zu; };
+// Kernel variants: 0-7 plain (read-only-cache neighbours), 8-23 TMA-pipelined
+// (need a row pitch that is a multiple of 16 bytes).  19-23 take two adjacent
+// x cells per thread (wv_tma_pair_kernel, pointwise ring of nq slots) and are
+// built for FP32 fields with at most two relaxation processes.
+struct Variant { int tx, ty, zb, tma, cpt, zu, pair, nq; };
 static const Variant kVariants[] = {
-    {32, 8, 32, 0, 1, 1}, {32, 4, 32, 0, 1, 1}, {64, 4, 32, 0, 1, 1}, {32, 8, 64, 0, 1, 1},
-    {32, 16, 16, 0, 1, 1}, {64, 8, 16, 0, 1, 1}, {128, 2, 32, 0, 1, 1}, {32, 8, 0, 0, 1, 1},
-    {32, 4, 32, 1, 1, 1}, {32, 8, 32, 1, 2, 1}, {32, 4, 24, 1, 1, 2}, {32, 4, 16, 1, 1, 1},
-    {32, 8, 16, 1, 1, 2}, {32, 4, 20, 1, 1, 2}, {32, 4, 32, 1, 1, 2}, {32, 8, 32, 1, 1, 1},
+    {32, 8, 32, 0, 1, 1, 0, 3}, {32, 4, 32, 0, 1, 1, 0, 3}, {64, 4, 32, 0, 1, 1, 0, 3}, {32, 8, 64, 0, 1, 1, 0, 3},
+    {32, 16, 16, 0, 1, 1, 0, 3}, {64, 8, 16, 0, 1, 1, 0, 3}, {128, 2, 32, 0, 1, 1, 0, 3}, {32, 8, 0, 0, 1, 1, 0, 3},
+    {32, 4, 32, 1, 1, 1, 0, 3}, {32, 8, 32, 1, 2, 1, 0, 3}, {32, 4, 24, 1, 1, 2, 0, 3}, {32, 4, 16, 1, 1, 1, 0, 3},
+    {32, 8, 16, 1, 1, 2, 0, 3}, {32, 4, 20, 1, 1, 2, 0, 3}, {32, 4, 32, 1, 1, 2, 0, 3}, {32, 8, 32, 1, 1, 1, 0, 3},
     // zb = -1: z-chunk fitted so the grid fills a whole number of waves
-    {32, 8, -1, 1, 1, 2}, {32, 4, -1, 1, 1, 1}, {32, 4, -1, 1, 1, 2},
+    {32, 8, -1, 1, 1, 2, 0, 3}, {32, 4, -1, 1, 1, 1, 0, 3}, {32, 4, -1, 1, 1, 2, 0, 3},
+    // two x cells per thread, two-slot pointwise ring
+    {32, 8, -1, 1, 1, 1, 1, 2}, {32, 8, -1, 1, 1, 2, 1, 2}, {64, 8, -1, 1, 1, 1, 1, 2},
+    {64, 8, -1, 1, 1, 2, 1, 2}, {32, 16, -1, 1, 1, 1, 1, 2},
 };
 static const int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
@@ -200,6 +206,13 @@ static bool tma_eligible(const WvSession& S) {
     return (S.nx * S.esz) % 16 == 0 && S.nx >= 8;
 }
 
+// The two-cell variants are compiled for FP32 fields with at most two
+// relaxation processes; a 16-byte row pitch makes nx even.
+static bool variant_ok(const WvSession& S, int v) {
+    if (!kVariants[v].pair) return true;
+    return S.prec == BD_F32 && S.max_relax <= 2 && tma_eligible(S);
+}
+
 static void build_maps(WvSession& S, int tx, int ty) {
     if (S.maps_tx == tx && S.maps_ty == ty) return;
     const bool f = S.prec == BD_F32;
@@ -261,10 +274,9 @@ static void launch_tma_k(WvSession& S, const WvArgs<real>& a0, const TmaMaps& ma
     BD_LAUNCHED(S.ctx);
 }
 
-template <class real, int TX, int TY, int CPT, int ZU>
-static void launch_tma_t(WvSession& S, const WvArgs<real>& a, int64_t s, int koff, cudaStream_t st) {
-    build_maps(S, TX, TY);
-    TmaMaps maps;
+// Tensor maps of step s: p^n with its halo, p^{n-1..n-4}, R, peak, energy, c.
+static void step_maps(WvSession& S, int64_t s, int tx, int ty, TmaMaps& maps) {
+    build_maps(S, tx, ty);
     std::memset(&maps, 0, sizeof maps);
     const int h = head_of(s);
     maps.p0 = S.mP0[h];
@@ -278,6 +290,12 @@ static void launch_tma_t(WvSession& S, const WvArgs<real>& a, int64_t s, int kof
     maps.peak = S.mPeak;
     maps.energy = S.mEnergy;
     if (S.has_cmap) maps.cmap = S.mC;
+}
+
+template <class real, int TX, int TY, int CPT, int ZU>
+static void launch_tma_t(WvSession& S, const WvArgs<real>& a, int64_t s, int koff, cudaStream_t st) {
+    TmaMaps maps;
+    step_maps(S, s, TX, TY, maps);
     // FP32 kernels with 0, 1 or 2 relaxation processes are compiled for their count;
     // FP64 and larger counts use the kernel that reads the count at run time
     if (sizeof(real) == 4 && S.max_relax == 0) launch_tma_k<real, TX, TY, CPT, 0, ZU>(S, a, maps, koff, st);
@@ -286,6 +304,34 @@ static void launch_tma_t(WvSession& S, const WvArgs<real>& a, int64_t s, int kof
     else if (sizeof(real) == 4 && S.max_relax == 1) launch_tma_k<real, TX, TY, CPT, 1, ZU>(S, a, maps, koff, st);
     else if (sizeof(real) == 4 && S.max_relax == 2) launch_tma_k<real, TX, TY, CPT, 2, ZU>(S, a, maps, koff, st);
     else launch_tma_k<real, TX, TY, CPT, -1, ZU>(S, a, maps, koff, st);
+}
+
+// Two x cells per thread (FP32; variant_ok has been checked).
+template <class real>
+static void launch_pair(WvSession& S, const WvArgs<real>& a, int64_t s, int koff, cudaStream_t st, const Variant& v) {
+    if constexpr (sizeof(real) != 4) {
+        fail(BD_ERR_INVALID_ARG, "two-cell tile variants take FP32 fields");
+    } else {
+        TmaMaps maps;
+        step_maps(S, s, v.tx, v.ty, maps);
+        PairCall c;
+        c.ctx = S.ctx;
+        c.a = &a;
+        c.K = S.kconst.as<WvConst<float>>();
+        c.koff = koff;
+        c.maps = &maps;
+        c.err = S.flag.as<unsigned>() + 1;
+        c.pdl = &S.pdl;
+        c.st = st;
+        c.tx = v.tx;
+        c.ty = v.ty;
+        c.zu = v.zu;
+        c.nq = v.nq;
+        c.kind = S.max_relax == 0 ? 0
+                 : S.max_relax == 1 ? ((S.has_cmap && !S.has_matmap && !S.has_planemat) ? 1 : 2)
+                 : S.max_relax == 2 ? 3 : -1;
+        wv_pair_launch(c);
+    }
 }
 
 template <class real, int TX, int TY>
@@ -302,7 +348,10 @@ static void launch_step(WvSession& S, int variant, int64_t s, int koff, cudaStre
     const Variant& v = kVariants[variant];
     a.zb = v.zb > 0 ? v.zb : (v.zb < 0 && v.tma ? -1 : S.nz);
     if (v.tma && !tma_eligible(S)) fail(BD_ERR_INVALID_ARG, "tile variant %d needs a 16-byte row pitch", variant);
-    switch (variant) {
+    if (!variant_ok(S, variant))
+        fail(BD_ERR_INVALID_ARG, "tile variant %d takes FP32 fields with at most two relaxation processes", variant);
+    if (v.pair) launch_pair<real>(S, a, s, koff, st, v);
+    else switch (variant) {
         case 0: case 3: case 7: launch_step_t<real, 32, 8>(S, a, koff, st); break;
         case 1: launch_step_t<real, 32, 4>(S, a, koff, st); break;
         case 2: launch_step_t<real, 64, 4>(S, a, koff, st); break;
@@ -470,6 +519,7 @@ static void autotune(WvSession& S) {
         for (int v = 0; v < kNumVariants; ++v) {
             if (kVariants[v].zb == 0 && S.nz > 512) continue;
             if (kVariants[v].tma && !tma_eligible(S)) continue;
+            if (!variant_ok(S, v)) continue;
             issue_steps(S, v, S.step, 2, st);  // warm-up
             S.step += 2;
             BD_CUDA(cudaEventRecord(S.ctx->ev0, st));

@@ -431,7 +431,7 @@ __global__ void wv_mur_y_kernel(const WvArgs<real> a, const WvConst<real>* __res
     }
 }
 
-__global__ void wv_advance_kernel(long long* step_base, int n) {
+static __global__ void wv_advance_kernel(long long* step_base, int n) {
     if (threadIdx.x == 0 && blockIdx.x == 0) *step_base += n;
 }
 

@@ -97,7 +97,7 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, u
 
 // Shared-memory layout.  NRMAX is the number of relaxation processes the slot
 // has room for (the compile-time count, or BD_MAX_RELAX for the generic kernel).
-template <class real, int TX, int TY, int NRMAX>
+template <class real, int TX, int TY, int NRMAX, int NQ = TMA_NQ>
 struct TmaLayout {
     static constexpr int PW = TX + 8, PH = TY + 6;
     static constexpr int PT = PW * PH;
@@ -108,7 +108,7 @@ struct TmaLayout {
     static constexpr int NQR = 4 + 2 * NRMAX + 2;                                 // real tiles per slot
     static constexpr int QS = NQR * QTB + QTF;                                    // slot bytes
     static constexpr int K_PEAK = 4 + 2 * NRMAX, K_ENERGY = 5 + 2 * NRMAX;
-    static constexpr int SMEM = TMA_NP * PSLOT + TMA_NQ * QS + (TMA_NP + TMA_NQ) * 8;
+    static constexpr int SMEM = TMA_NP * PSLOT + NQ * QS + (TMA_NP + NQ) * 8;
 };
 
 // One Westervelt step, TMA-pipelined.  Template parameters: tile TX x TY, CPT

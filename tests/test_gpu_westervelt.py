@@ -98,7 +98,7 @@ def test_graph_and_plain_launches_identical(ctx):
 def test_all_tile_variants_identical(ctx):
     """Plain and TMA-pipelined kernels, every tile shape: bitwise-identical fields."""
     base = None
-    for v in range(19):
+    for v in range(24):
         p = presets.cfg1(40, 40, 72, 60, precision=abi.BD_F32)
         p.params.tile_variant = v
         r = ctx.westervelt(p, want=("p_final", "peak"))
@@ -107,6 +107,28 @@ def test_all_tile_variants_identical(ctx):
         else:
             np.testing.assert_array_equal(r["p_final"], base["p_final"])
             np.testing.assert_array_equal(r["peak"], base["peak"])
+
+
+def test_two_cell_variants_on_reference_physics(ctx):
+    """The two-x-cells-per-thread variants on the reference's setup (mirror
+    planes, Mur faces, source plane, water/tissue planes with two relaxation
+    processes, the harmonic DFT): every output equal to the plain kernel's.
+    nx = 28 is not a multiple of the 32- or 64-cell tiles, so the last tile column is
+    partly outside the grid; FP64 fields are refused by these variants."""
+    base = None
+    for v in (0, 16, 19, 20, 21, 22, 23):
+        p = presets.ref_W_mini(abi.BD_F32, Nxy=28, Nz=40, loop1_periods=1, periods=1)
+        p.params.tile_variant = v
+        r = ctx.westervelt(p)
+        if base is None:
+            base = r
+            continue
+        for k in ("p_final", "peak", "energy", "Q", "dft_re", "dft_im"):
+            np.testing.assert_array_equal(r[k], base[k], err_msg="variant %d, %s" % (v, k))
+    p64 = presets.ref_W_mini(abi.BD_F64, Nxy=28, Nz=40, loop1_periods=1, periods=1)
+    p64.params.tile_variant = 19
+    with pytest.raises(api.BDError):
+        ctx.westervelt(p64)
 
 
 def test_run_twice_bitwise(ctx):
