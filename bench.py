@@ -40,10 +40,11 @@ CFG1 = dict(nx=128, ny=128, nz=256, n_steps=3000)
 BYTES_PER_CELL = 56          # p^n..p^{n-4} 20 B, p^{n+1} 4, R 12, c 4, peak 8, energy 8
 METRIC = "Westervelt Gcell-updates/s"
 UNIT = "Gcell-updates/s"
-# dram__bytes_read.sum + dram__bytes_write.sum of one wv_tma_kernel launch on the
-# cfg1 grid (mean of the two launches of the ncu capture of tile variant 16;
-# summary in profiles/westervelt_cfg1_wv_tma_kernel.md)
-NCU_TRAFFIC_BYTES = 201566336
+# dram__bytes_read.sum + dram__bytes_write.sum of one step-kernel launch on the
+# cfg1 grid (first launch of the ncu capture of tile variant 21, the
+# wv_tma_pair_kernel the autotuner picks; summary in
+# profiles/westervelt_cfg1_wv_tma_pair_kernel.md)
+NCU_TRAFFIC_BYTES = 202600192
 
 
 def peaks():
@@ -253,7 +254,7 @@ def run_westervelt(args, world, rank, local):
     cmap = prob.array("c_map")
     h2d = cmap.nbytes + prob.grid.nx * prob.grid.ny * (4 + 4 * 4 + 4) + T * (8 + 16 + 4)
     d2h = 2 * ncell * 4
-    ctx.westervelt(prob, want=("peak", "energy"))   # warm
+    warm = ctx.westervelt(prob, want=("peak", "energy"))   # warm; the variant the tuner chose
     dist_barrier(world)
     t0 = time.perf_counter()
     for _ in range(args.steps):
@@ -271,7 +272,8 @@ def run_westervelt(args, world, rank, local):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": "cfg1 plain Westervelt FP32 128x128x256, 3000 time steps per step",
                    "grid": [128, 128, 256], "time_steps_per_step": T, "dx_mm": 0.1875, "relax_processes": 1,
-                   "sponge_cells": 20, "parallelism": "replicas" if world > 1 else "single GPU",
+                   "sponge_cells": 20, "tile_variant": int(warm["tile_variant"]),
+                   "parallelism": "replicas" if world > 1 else "single GPU",
                    "l2": "inputs larger than L2 (about 170 MB of fields streamed per time step)"},
         "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk.summary(),
         "gpu_launches": int(launches),

@@ -133,7 +133,7 @@ class WesterveltOutputs(C.Structure):
     _fields_ = [
         ("p_final", vp), ("peak", vp), ("energy", vp),
         ("dft_re", vp), ("dft_im", vp), ("Q", vp),
-        ("elapsed_ms", f64), ("steps_done", i64),
+        ("elapsed_ms", f64), ("steps_done", i64), ("tile_variant", i32), ("pad0", i32),
     ]
 
 

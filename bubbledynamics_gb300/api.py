@@ -233,6 +233,7 @@ class Context:
                 res[k] = res[k].reshape(prob.shape)
         res["elapsed_ms"] = out.elapsed_ms
         res["steps_done"] = out.steps_done
+        res["tile_variant"] = out.tile_variant
         return res
 
     def westervelt(self, prob: WesterveltProblem, want=("p_final", "peak", "energy", "Q", "dft")):

@@ -840,6 +840,7 @@ static void finish(WvSession& S, bd_westervelt_outputs* o) {
         BD_CUDA(cudaStreamSynchronize(st));
     }
     o->steps_done = S.step;
+    o->tile_variant = S.variant;
 }
 
 // ---------------------------------------------------------------- checkpoint

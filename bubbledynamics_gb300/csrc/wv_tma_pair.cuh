@@ -364,7 +364,36 @@ __global__ void __launch_bounds__(TX* TY / 2, 1536 / (TX * TY)) wv_tma_pair_kern
                     for (int cx = 0; cx < CX; ++cx)
                         if (acc[cx]) enz[col[c0 + cx]] = ev[cx];
             }
-            if (do_dft && iz >= a.dz_lo && iz < a.dz_hi) {
+            if (do_dft && iz >= a.dz_lo && iz < a.dz_hi && acc_pair) {
+                // both cells accumulate: one pair load and store per accumulator
+                using P2 = typename Pair<real>::T;
+                const long long pl = (long long)(iz - a.dz_lo) * a.plane + col[c0];
+                const long long stride = (long long)(a.dz_hi - a.dz_lo) * a.plane;
+                const real* tw = a.tw + ds * a.n_dft * 2;
+                real* dr = a.dre + pl;
+                real* di = a.dim + pl;
+                int j = 0;
+                for (; j + 4 <= a.n_dft; j += 4) {
+                    P2 r[4], m[4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        r[u] = *reinterpret_cast<const P2*>(dr + (j + u) * stride);
+                        m[u] = *reinterpret_cast<const P2*>(di + (j + u) * stride);
+                    }
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const real tr = tw[2 * (j + u)], ti = tw[2 * (j + u) + 1];
+                        st2(dr + (j + u) * stride, fma_(pn[0], tr, r[u].x), fma_(pn[1], tr, r[u].y));
+                        st2(di + (j + u) * stride, fma_(-pn[0], ti, m[u].x), fma_(-pn[1], ti, m[u].y));
+                    }
+                }
+                for (; j < a.n_dft; ++j) {
+                    const P2 r = *reinterpret_cast<const P2*>(dr + j * stride);
+                    const P2 m = *reinterpret_cast<const P2*>(di + j * stride);
+                    st2(dr + j * stride, fma_(pn[0], tw[2 * j], r.x), fma_(pn[1], tw[2 * j], r.y));
+                    st2(di + j * stride, fma_(-pn[0], tw[2 * j + 1], m.x), fma_(-pn[1], tw[2 * j + 1], m.y));
+                }
+            } else if (do_dft && iz >= a.dz_lo && iz < a.dz_hi) {
 #pragma unroll
                 for (int cx = 0; cx < CX; ++cx) {
                     if (!acc[cx]) continue;

@@ -196,6 +196,8 @@ typedef struct bd_westervelt_outputs {
     double* Q;                  /* nx*ny*nz acoustic power density [W/m^3] (BD_Q_REFERENCE) */
     double elapsed_ms;          /* device time of the solve (filled by the library) */
     int64_t steps_done;
+    int32_t tile_variant;       /* step-kernel variant the solve ran (filled by the library) */
+    int32_t pad0;
 } bd_westervelt_outputs;
 
 /* Full Westervelt solve.  Replaces W:350-790 (the three time loops, the FFT
