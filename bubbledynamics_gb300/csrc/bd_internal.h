@@ -125,10 +125,12 @@ void ctx_check(bd_context* ctx);
 // resident CTAs (at least `fill` of the last wave busy), the largest such
 // chunk of at least 8 planes with the chunk count rounded up to cover w waves;
 // failing that, the chunk count rounded down (just under w waves); 16 if
-// neither qualifies.
-inline int wave_fitted_zb(long long tiles, int nz, long long slots, double fill = 0.97) {
-    for (int down = 0; down < 2; ++down)
+// neither qualifies.  down_first tries the rounded-down counts first (fewer,
+// longer chunks, for kernels with a long per-chunk prologue).
+inline int wave_fitted_zb(long long tiles, int nz, long long slots, double fill = 0.97, bool down_first = false) {
+    for (int pass = 0; pass < 2; ++pass)
         for (int w = 1; w <= 16; ++w) {
+            const bool down = (pass == 0) == down_first;
             const long long chunks = down ? (w * slots) / tiles : (w * slots + tiles - 1) / tiles;
             if (chunks > nz) break;
             if (chunks < 1) continue;

@@ -83,6 +83,9 @@ struct WvSession {
     int graph_variant = -1;
     // tensor maps of the TMA variant in use (built per tile shape)
     int maps_tx = 0, maps_ty = 0;
+    // adjoint: TMA map of the H buffer for the stencil pass (valid while adj_tma)
+    CUtensorMap adj_mapH;
+    bool adj_tma = false;
     CUtensorMap mP0[5], mQ[5], mR[BD_MAX_RELAX][2], mC, mPeak, mEnergy;
     // segment view (TMA variants only): the pressure levels of the next step are
     // read from, and p^{n+1} written to, caller-chosen buffers instead of the ring
@@ -922,6 +925,28 @@ static void adj_launch_n(WvSession& S, const AdjArgs<real>& a, cudaStream_t st) 
     }
     BD_LAUNCHED(S.ctx);
     if constexpr (sizeof(real) == 4) {
+        if (S.adj_tma) {
+            // H planes streamed by TMA, z-chunk fitted to whole waves of resident CTAs
+            // (on cfg4 this pass takes 25 us of the 106 us backward step; the pointwise
+            // pass streams at 0.91 of HBM)
+            constexpr int TX = 64, TY = 8, NPA = 8;
+            using LA = AdjTmaLayout<TX, TY, NPA>;
+            static int per_sm = 0;
+            if (!per_sm) {
+                BD_CUDA(cudaFuncSetAttribute(adj_stencil_tma_kernel<TX, TY, NPA>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, LA::SMEM));
+                BD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, adj_stencil_tma_kernel<TX, TY, NPA>,
+                                                                      TX * TY / 2, LA::SMEM));
+            }
+            AdjArgs<real> at = a;
+            const long long tiles = (long long)((S.nx + TX - 1) / TX) * ((S.ny + TY - 1) / TY);
+            // fewer, longer chunks: each chunk first fills its six-plane z window
+            at.zb = wave_fitted_zb(tiles, S.nz, (long long)S.ctx->sm_count * std::max(per_sm, 1), 0.9, true);
+            dim3 b(TX / 2, TY), g((S.nx + TX - 1) / TX, (S.ny + TY - 1) / TY, (S.nz + at.zb - 1) / at.zb);
+            adj_stencil_tma_kernel<TX, TY, NPA><<<g, b, LA::SMEM, st>>>(at, S.adj_mapH, S.flag.as<unsigned>() + 1);
+            BD_LAUNCHED(S.ctx);
+            return;
+        }
         if (S.nx % 4 == 0) {
             // z-chunk fitted to whole waves of the four-cell kernel's resident CTAs
             static int per_sm = 0;
@@ -1045,6 +1070,13 @@ static void adjoint_solve(WvSession& S, const bd_focal_loss* loss, double* loss_
     // backward buffers
     PoolBuf mu[6], muR[BD_MAX_RELAX][3], gphi, gamp, eamp, H;
     H.alloc(S.ctx, f);
+    // FP32 stencil pass with TMA-streamed H planes where the row pitch allows it
+    S.adj_tma = S.prec == BD_F32 && tma_eligible(S);
+    if (S.adj_tma) S.adj_mapH = make_map(S, H.p, true, 64 + 8, 8 + 6);
+    struct AdjTmaOff {
+        WvSession& s;
+        ~AdjTmaOff() { s.adj_tma = false; }
+    } adj_tma_off{S};
     for (auto& b : mu) { b.alloc(S.ctx, f); BD_CUDA(cudaMemsetAsync(b.p, 0, f, st)); }
     for (int v = 0; v < S.max_relax; ++v)
         for (auto& b : muR[v]) { b.alloc(S.ctx, f); BD_CUDA(cudaMemsetAsync(b.p, 0, f, st)); }
@@ -1148,6 +1180,11 @@ static void adjoint_solve(WvSession& S, const bd_focal_loss* loss, double* loss_
     }
     S.p = saved;
     S.n_dft = n_dft_saved;
+    {
+        unsigned fl = 0;   // bounded pipeline waits of the forward and stencil kernels
+        BD_CUDA(cudaMemcpy(&fl, S.flag.as<unsigned>() + 1, sizeof fl, cudaMemcpyDeviceToHost));
+        if (fl & 4u) fail(BD_ERR_TIMEOUT, "a pipeline wait of the adjoint solve timed out");
+    }
     // per-element sums of the per-cell gradients
     std::vector<double> gp(S.plane), ga(S.plane);
     BD_CUDA(cudaMemcpy(gp.data(), gphi.p, S.plane * 8, cudaMemcpyDeviceToHost));

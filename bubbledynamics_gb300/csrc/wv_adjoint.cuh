@@ -16,6 +16,8 @@
 // relaxation adjoints rotate through three buffers per process.
 #pragma once
 
+#include "wv_tma.cuh"
+
 #include "wv_kernels.cuh"
 
 namespace bd {
@@ -456,6 +458,130 @@ __global__ void __launch_bounds__(128) adj_stencil4_kernel(const AdjArgs<float> 
         *reinterpret_cast<float4*>(lam + i) = make_float4(out[0], out[1], out[2], out[3]);
 #pragma unroll
         for (int k = 0; k < 6; ++k) w[k] = w[k + 1];
+    }
+}
+
+// The same stencil pass with the H planes streamed by TMA: a CTA owns TX x TY
+// columns (two adjacent x cells per thread) and a z-chunk; one elected thread
+// keeps a ring of ADJ_NP (>= 7) plane tiles of H with their halo ((TX+8) x (TY+6),
+// x from 4 cells left of the block so the TMA x coordinate stays 16-byte
+// aligned; out-of-grid cells arrive as zeros, the stencil's ghost value) up to
+// ADJ_NP - 4 planes ahead, threads keep H(iz-3..iz+3) of their cells in registers,
+// and lambda_0 is read and written as one 8-byte pair per thread.  Needs a
+// row pitch that is a multiple of 16 bytes (nx % 4 == 0).  Waits are bounded
+// (bit 4 of *err, as in the forward kernels).
+template <int TX, int TY, int ADJ_NP = 8>
+struct AdjTmaLayout {
+    static constexpr int PW = TX + 8, PH = TY + 6;
+    static constexpr int PSLOT = ((PW * PH * 4 + 127) / 128) * 128;
+    static constexpr int SMEM = ADJ_NP * PSLOT + ADJ_NP * 8;
+};
+
+template <int TX, int TY, int ADJ_NP = 8>
+__global__ void __launch_bounds__(TX* TY / 2, 4) adj_stencil_tma_kernel(const AdjArgs<float> a,
+                                                                        const __grid_constant__ CUtensorMap mapH,
+                                                                        unsigned* __restrict__ err) {
+    using L = AdjTmaLayout<TX, TY, ADJ_NP>;
+    constexpr int TXT = TX / 2;
+    extern __shared__ __align__(128) unsigned char smem[];
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + ADJ_NP * L::PSLOT);
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int tid = ty * TXT + tx;
+    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
+    const int z0 = blockIdx.z * a.zb;
+    const int z1 = min(a.nz, z0 + a.zb);
+    const int zbn = z1 - z0;
+    auto slot = [&](int q) { return reinterpret_cast<const float*>(smem + (q % ADJ_NP) * L::PSLOT); };
+    auto issue = [&](int q) {                      // plane z0 - 3 + q of H
+        if (q > zbn + 5) return;
+        const int plane = z0 - 3 + q;
+        uint64_t* b = &bar[q % ADJ_NP];
+        if (plane < 0 || plane >= a.nz) { mbar_arrive(b); return; }   // read as zeros, nothing to copy
+        mbar_expect_tx(b, L::PW * L::PH * 4u);
+        tma_load_3d(smem + (q % ADJ_NP) * L::PSLOT, &mapH, b, x0 - 4, y0 - 3, plane);
+    };
+    auto wait = [&](int q) { mbar_wait(&bar[q % ADJ_NP], (unsigned)((q / ADJ_NP) & 1), err); };
+    if (tid == 0) {
+        for (int s = 0; s < ADJ_NP; ++s) mbar_init(&bar[s], 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    if (tid == 0)
+        for (int q = 0; q < ADJ_NP; ++q) issue(q);
+    const int lx = 2 * tx;
+    const int ix = x0 + lx, iy = y0 + ty;
+    const bool active = ix < a.nx && iy < a.ny;
+    const int own = (ty + 3) * L::PW + lx + 4;
+    const long long col = (long long)iy * a.nx + ix;
+    float w[2][7];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {                  // planes z0-3 .. z0+2
+        wait(k);
+        const int plane = z0 - 3 + k;
+        const bool in = plane >= 0 && plane < a.nz;
+        const float2 v = *reinterpret_cast<const float2*>(slot(k) + own);
+        w[0][k] = in ? v.x : 0.f;
+        w[1][k] = in ? v.y : 0.f;
+    }
+    __syncthreads();                               // slots of planes z0-3 .. z0-1 are free again
+    if (tid == 0)
+        for (int q = ADJ_NP; q < ADJ_NP + 3; ++q) issue(q);
+    // lambda_0 is read two planes ahead (registers), so its latency overlaps two planes of work
+    float* const lam0 = a.mu[1] + col;
+    auto lam_at = [&](int z) -> float2 {
+        return (active && z < z1) ? *reinterpret_cast<const float2*>(lam0 + (long long)z * a.plane)
+                                  : make_float2(0.f, 0.f);
+    };
+    float2 lnext[2] = {lam_at(z0), lam_at(z0 + 1)};
+    for (int iz = z0; iz < z1; ++iz) {
+        const int qc = iz - z0 + 3;
+        float* lam = lam0 + (long long)iz * a.plane;
+        const float2 l = lnext[0];
+        lnext[0] = lnext[1];
+        lnext[1] = lam_at(iz + 2);
+        wait(qc + 3);
+        {
+            const bool in = iz + 3 < a.nz;
+            const float2 v = *reinterpret_cast<const float2*>(slot(qc + 3) + own);
+            w[0][6] = in ? v.x : 0.f;
+            w[1][6] = in ? v.y : 0.f;
+        }
+        if (active) {
+            const float* c0 = slot(qc) + own;
+            constexpr int W = L::PW;
+            float xs[10];                          // x offsets -4 .. +5 from the first cell
+#pragma unroll
+            for (int j = 0; j < 5; ++j) {
+                const float2 v = *reinterpret_cast<const float2*>(c0 - 4 + 2 * j);
+                xs[2 * j] = v.x;
+                xs[2 * j + 1] = v.y;
+            }
+            float yp[3][2], ym[3][2];
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                const float2 u = *reinterpret_cast<const float2*>(c0 + (j + 1) * W);
+                const float2 v = *reinterpret_cast<const float2*>(c0 - (j + 1) * W);
+                yp[j][0] = u.x; yp[j][1] = u.y;
+                ym[j][0] = v.x; ym[j][1] = v.y;
+            }
+            const float lin[2] = {l.x, l.y};
+            float out[2];
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                const float ax1 = xs[5 + k] + xs[3 + k], ax2 = xs[6 + k] + xs[2 + k], ax3 = xs[7 + k] + xs[1 + k];
+                const float h0 = w[k][3];
+                const float sxy = -980.f * h0 + 270.f * (ax1 + (yp[0][k] + ym[0][k])) -
+                                  27.f * (ax2 + (yp[1][k] + ym[1][k])) + 2.f * (ax3 + (yp[2][k] + ym[2][k]));
+                const float sz = -490.f * h0 + 270.f * (w[k][4] + w[k][2]) - 27.f * (w[k][5] + w[k][1]) +
+                                 2.f * (w[k][6] + w[k][0]);
+                out[k] = lin[k] + a.kxy180 * sxy + a.kz180 * sz;
+            }
+            *reinterpret_cast<float2*>(lam) = make_float2(out[0], out[1]);
+        }
+#pragma unroll
+        for (int k = 0; k < 6; ++k) { w[0][k] = w[0][k + 1]; w[1][k] = w[1][k + 1]; }
+        __syncthreads();                           // plane qc's slot is free
+        if (tid == 0) issue(qc + ADJ_NP);
     }
 }
 
