@@ -131,6 +131,29 @@ def test_two_cell_variants_on_reference_physics(ctx):
         ctx.westervelt(p64)
 
 
+def test_two_cell_variants_with_per_cell_materials(ctx):
+    """A per-cell material map mixing water (no relaxation) and tissue (two
+    processes) cell by cell, so the two cells of a thread often differ in
+    material and relaxation count: every tile variant, including the paired
+    ones, gives the plain kernel's bits."""
+    base = None
+    rng = np.random.default_rng(11)
+    for v in (0, 16, 17, 19, 20, 21, 22, 23):
+        p = presets.ref_W_mini(abi.BD_F32, Nxy=32, Nz=40, loop1_periods=1, periods=1)
+        if base is None:
+            mm = (rng.random(p.shape) < 0.5).astype(np.uint8)
+        p.set_material_map(mm)
+        p.params.tile_variant = v
+        r = ctx.westervelt(p, want=("p_final", "peak", "energy"))
+        assert r["tile_variant"] == v
+        if base is None:
+            base = r
+            assert np.isfinite(base["p_final"]).all() and np.abs(base["p_final"]).max() > 0
+            continue
+        for k in ("p_final", "peak", "energy"):
+            np.testing.assert_array_equal(r[k], base[k], err_msg="variant %d, %s" % (v, k))
+
+
 def test_run_twice_bitwise(ctx):
     p = presets.ref_W_mini(abi.BD_F32, Nxy=24, Nz=40, loop1_periods=1, periods=1)
     a = ctx.westervelt(p)
