@@ -485,7 +485,8 @@ def run_gilmore(args):
     r, ms = ctx.gilmore(med, b, o)
     att = float(r["n_accept"].sum() + r["n_reject"].sum())
     print(json.dumps({"workload": "cfg2 Gilmore sample", "bubbles": args.bubbles, "t_end": args.t_end,
-                      "schedule": args.schedule, "ms": ms, "attempts_per_s": att / (ms * 1e-3)}), flush=True)
+                      "schedule": args.schedule, "ms": ms, "attempts": int(att),
+                      "attempts_per_s": att / (ms * 1e-3)}), flush=True)
     ctx.close()
 
 
