@@ -265,6 +265,8 @@ __global__ void __launch_bounds__(TX* TY / CPT) wv_tma_kernel(const WvArgs<real>
                     const int cc = e % L::PW, k = e / L::PW + 1;
                     T[(3 - k) * L::PW + cc] = T[(3 + k) * L::PW + cc];
                 }
+            // TMA refills this slot later: order these ordinary stores before that copy
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             __syncthreads();
         }
         waitQ(r);

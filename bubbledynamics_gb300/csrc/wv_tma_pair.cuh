@@ -196,6 +196,8 @@ __global__ void __launch_bounds__(TX* TY / 2, 1536 / (TX * TY)) wv_tma_pair_kern
                     const int cc = e % L::PW, k = e / L::PW + 1;
                     T[(3 - k) * L::PW + cc] = T[(3 + k) * L::PW + cc];
                 }
+            // TMA refills this slot later: order these ordinary stores before that copy
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             __syncthreads();
         }
         waitQ(r);
