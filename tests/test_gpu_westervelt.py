@@ -154,6 +154,34 @@ def test_two_cell_variants_with_per_cell_materials(ctx):
             np.testing.assert_array_equal(r[k], base[k], err_msg="variant %d, %s" % (v, k))
 
 
+@pytest.mark.parametrize("layout", ["no_relaxation", "plane_materials"])
+def test_two_cell_variants_material_layouts(ctx, layout):
+    """The paired kernel's other compile-time layouts on a cfg1 box: no
+    relaxation process at all, and one process with a second material by
+    planes (read per plane, no c-map shortcut).  Every variant gives the
+    plain kernel's bits."""
+    base = None
+    for v in (0, 17, 19, 20, 21, 22, 23):
+        p = presets.cfg1(40, 40, 72, 60, precision=abi.BD_F32)
+        if layout == "no_relaxation":
+            p.medium.mat[0].n_relax = 0
+        else:
+            m = p.medium.mat[0]
+            p.medium.n_materials = 2
+            p.medium.mat[1] = m
+            p.medium.mat[1].c0 = 1560.0
+            p.medium.mat[1].relax_c[0] = 8.0
+            p.set_plane_material([0 if iz < 36 else 1 for iz in range(72)])
+        p.params.tile_variant = v
+        r = ctx.westervelt(p, want=("p_final", "peak", "energy"))
+        if base is None:
+            base = r
+            assert np.abs(base["p_final"]).max() > 0
+            continue
+        for k in ("p_final", "peak", "energy"):
+            np.testing.assert_array_equal(r[k], base[k], err_msg="%s, variant %d, %s" % (layout, v, k))
+
+
 def test_run_twice_bitwise(ctx):
     p = presets.ref_W_mini(abi.BD_F32, Nxy=24, Nz=40, loop1_periods=1, periods=1)
     a = ctx.westervelt(p)
