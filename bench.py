@@ -523,8 +523,11 @@ def run_dft(args):
     from bubbledynamics_gb300 import api, presets
     ctx = api.Context(0)
     prob = presets.cfg5(nx=256, ny=256, nz=384, n_steps=args.time_steps, window_steps=args.time_steps)
+    if args.tile_variant >= 0:
+        prob.params.tile_variant = args.tile_variant
     r = ctx.westervelt(prob, want=("dft",))
     print(json.dumps({"workload": "cfg5 box in the DFT window", "time_steps": args.time_steps,
+                      "tile_variant": int(r["tile_variant"]),
                       "us_per_step": 1e3 * r["elapsed_ms"] / args.time_steps}), flush=True)
     ctx.close()
 
@@ -561,7 +564,8 @@ def main():
     ap.add_argument("--t-end", type=float, default=2e-6, help="gilmore workload: window [s]")
     ap.add_argument("--schedule", default="persistent", choices=["persistent", "static"])
     ap.add_argument("--time-steps", type=int, default=30, help="step-kernel workload: time steps per solve")
-    ap.add_argument("--tile-variant", type=int, default=-1, help="step-kernel workload: variant (-1: all TMA)")
+    ap.add_argument("--tile-variant", type=int, default=-1,
+                    help="step-kernel / dft workloads: tile variant (-1: every TMA variant / autotuned)")
     ap.add_argument("--cpu-sample", type=int, default=60)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extra", action="store_true", help="skip the adjoint and Gilmore summaries")
