@@ -55,6 +55,7 @@ def load(path=None):
     _sig(L, "bd_last_error_string", [], C.c_char_p)
     _sig(L, "bd_abi_version", [])
     _sig(L, "bd_context_kernel_launches", [P, C.POINTER(C.c_int64)])
+    _sig(L, "bd_selftest_bounded_wait", [P, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_double)])
     _sig(L, "bd_westervelt_run", [P, P, P, P, P, P])
     _sig(L, "bd_westervelt_begin", [P, P, P, P, P, C.POINTER(P)])
     _sig(L, "bd_westervelt_advance", [P, C.c_int64])
@@ -201,6 +202,13 @@ class Context:
         n = C.c_int64(0)
         check(self.L.bd_context_kernel_launches(self.h, C.byref(n)))
         return n.value
+
+    def selftest_bounded_wait(self, limit_ms=100):
+        """(timed_out, device ms) of a kernel whose pipeline wait nothing completes."""
+        t = C.c_int32(0)
+        ms = C.c_double(0)
+        check(self.L.bd_selftest_bounded_wait(self.h, int(limit_ms), C.byref(t), C.byref(ms)))
+        return bool(t.value), ms.value
 
     # ------------------------------------------------------------ Westervelt
     @staticmethod

@@ -1203,6 +1203,23 @@ static void adjoint_solve(WvSession& S, const bd_focal_loss* loss, double* loss_
 
 }  // namespace bd
 
+namespace bd {
+
+// Self-test of the bounded pipeline wait: one warp waits on an mbarrier that
+// nothing arrives on; the wait gives up after limit_ns, sets bit 4 of *err
+// (as a stalled TMA pipeline would) and the kernel returns.
+__global__ void wait_selftest_kernel(unsigned* err, unsigned long long limit_ns) {
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    mbar_wait_for(&bar, 0u, err, limit_ns);
+}
+
+}  // namespace bd
+
 struct bd_westervelt {
     bd::WvSession S;
 };
@@ -1225,6 +1242,28 @@ static double timed_advance(WvSession& S, int64_t n) {
 }
 
 extern "C" {
+
+bd_status bd_selftest_bounded_wait(bd_context* ctx, int32_t limit_ms, int32_t* timed_out, double* elapsed_ms) {
+    return guard([&] {
+        ctx_check(ctx);
+        if (limit_ms < 1 || limit_ms > 2000 || !timed_out) fail(BD_ERR_INVALID_ARG, "limit_ms must be 1..2000");
+        PoolBuf f;
+        f.alloc(ctx, 64);
+        cudaStream_t st = ctx->stream;
+        BD_CUDA(cudaMemsetAsync(f.p, 0, 64, st));
+        BD_CUDA(cudaEventRecord(ctx->ev0, st));
+        wait_selftest_kernel<<<1, 32, 0, st>>>(f.as<unsigned>(), (unsigned long long)limit_ms * 1000000ull);
+        BD_LAUNCHED(ctx);
+        BD_CUDA(cudaEventRecord(ctx->ev1, st));
+        unsigned flag = 0;
+        BD_CUDA(cudaMemcpyAsync(&flag, f.p, sizeof flag, cudaMemcpyDeviceToHost, st));
+        BD_CUDA(cudaStreamSynchronize(st));
+        float ms = 0;
+        BD_CUDA(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+        *timed_out = (flag & 4u) ? 1 : 0;
+        if (elapsed_ms) *elapsed_ms = ms;
+    });
+}
 
 bd_status bd_westervelt_begin(bd_context* ctx, const bd_grid* grid, const bd_medium* medium, const bd_source* source,
                               const bd_westervelt_params* params, bd_westervelt** out) {

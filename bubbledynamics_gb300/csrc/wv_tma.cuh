@@ -72,20 +72,25 @@ __device__ __forceinline__ unsigned long long global_ns() {
     return t;
 }
 
-// Bounded wait: gives up after two seconds, records the timeout in *err
+// Bounded wait: gives up after two seconds (mbar_wait_for: after limit_ns), records the timeout in *err
 // (bit 4) and returns false so the kernel can finish instead of hanging.
 // Once any wait has timed out, later waits return at once, so a broken
 // pipeline ends the kernel quickly.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, unsigned* err) {
+__device__ __forceinline__ bool mbar_wait_for(uint64_t* bar, unsigned parity, unsigned* err,
+                                              unsigned long long limit_ns) {
     if (mbar_try_wait(bar, parity)) return true;
     const unsigned long long t0 = global_ns();
     while (true) {
         if (mbar_try_wait(bar, parity)) return true;
         if (*reinterpret_cast<volatile unsigned*>(err) & 4u) return false;
-        if (global_ns() - t0 > 2000000000ull) break;
+        if (global_ns() - t0 > limit_ns) break;
     }
     atomicOr(err, 4u);
     return false;
+}
+
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, unsigned* err) {
+    return mbar_wait_for(bar, parity, err, 2000000000ull);
 }
 
 __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y, int z) {

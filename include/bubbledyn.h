@@ -72,6 +72,12 @@ const char* bd_last_error_string(void);
 int bd_abi_version(void);
 /* Number of this library's own kernels launched by the context so far. */
 bd_status bd_context_kernel_launches(bd_context* ctx, int64_t* out);
+/* Self-test of the bounded waits that guard every TMA pipeline in the step
+ * kernels (a stalled pipeline ends the kernel with BD_ERR_TIMEOUT instead of
+ * hanging): one warp waits on a barrier that nothing completes.  *timed_out is
+ * 1 when the wait gave up after limit_ms (1..2000) as designed; *elapsed_ms
+ * gets the kernel's device time.  The context stays usable afterwards. */
+bd_status bd_selftest_bounded_wait(bd_context* ctx, int32_t limit_ms, int32_t* timed_out, double* elapsed_ms);
 
 /* ------------------------------------------------------------------------- */
 /* Westervelt pressure / energy solver (W)                                    */

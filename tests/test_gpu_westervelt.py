@@ -182,6 +182,22 @@ def test_two_cell_variants_material_layouts(ctx, layout):
             np.testing.assert_array_equal(r[k], base[k], err_msg="%s, variant %d, %s" % (layout, v, k))
 
 
+def test_bounded_wait_gives_up_and_context_survives(ctx):
+    """The wait that guards every TMA pipeline slot, on a barrier nothing
+    completes: it gives up after its limit and records the timeout instead of
+    hanging, and the context then runs a solve with the same bits as before."""
+    p = presets.ref_W_mini(abi.BD_F32, Nxy=24, Nz=40, loop1_periods=1, periods=1)
+    before = ctx.westervelt(p)
+    timed_out, ms = ctx.selftest_bounded_wait(100)
+    assert timed_out
+    assert 90.0 <= ms < 2000.0
+    after = ctx.westervelt(p)
+    for k in ("p_final", "Q"):
+        np.testing.assert_array_equal(after[k], before[k])
+    with pytest.raises(api.BDError):
+        ctx.selftest_bounded_wait(0)
+
+
 def test_run_twice_bitwise(ctx):
     p = presets.ref_W_mini(abi.BD_F32, Nxy=24, Nz=40, loop1_periods=1, periods=1)
     a = ctx.westervelt(p)
