@@ -42,8 +42,7 @@ METRIC = "Westervelt Gcell-updates/s"
 UNIT = "Gcell-updates/s"
 # dram__bytes_read.sum + dram__bytes_write.sum of one step-kernel launch on the
 # cfg1 grid (first launch of the ncu capture of tile variant 21, the
-# wv_tma_pair_kernel the autotuner picks; summary in
-# profiles/westervelt_cfg1_wv_tma_pair_kernel.md)
+# wv_tma_pair_kernel the autotuner picks)
 NCU_TRAFFIC_BYTES = 202600192
 
 

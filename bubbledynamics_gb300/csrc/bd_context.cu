@@ -102,6 +102,7 @@ bd_status bd_context_create(int device, bd_context** out) {
         BD_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
         BD_CUDA(cudaEventCreate(&c->ev0));
         BD_CUDA(cudaEventCreate(&c->ev1));
+        BD_CUDA(cudaMalloc(&c->gil_counter, 256));
         *out = c;
     });
 }
@@ -112,6 +113,7 @@ bd_status bd_context_destroy(bd_context* ctx) {
         cudaSetDevice(ctx->device);
         if (ctx->stream) cudaStreamSynchronize(ctx->stream);
         pool_trim(ctx);
+        if (ctx->gil_counter) cudaFree(ctx->gil_counter);
         if (ctx->ev0) cudaEventDestroy(ctx->ev0);
         if (ctx->ev1) cudaEventDestroy(ctx->ev1);
         if (ctx->stream) cudaStreamDestroy(ctx->stream);

@@ -747,10 +747,9 @@ bd_status bd_gilmore_run_device(bd_context* ctx, const bd_gilmore_medium* medium
         if (n < 0 || (n > 0 && (!d_bubbles || !d_results))) fail(BD_ERR_INVALID_ARG, "bad bubble arrays");
         if (n == 0) return;
         cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
-        // the work counter lives in a small block owned by the context's pool
-        static thread_local PoolBuf counter;
-        if (!counter.p || counter.ctx != ctx) counter.alloc(ctx, 64);
-        launch_run(ctx, medium, n, d_bubbles, ode, d_results, counter.as<unsigned long long>(), st);
+        // the persistent schedule's work counter belongs to the context (one per
+        // context: calls on different streams whose work overlaps must be serialised)
+        launch_run(ctx, medium, n, d_bubbles, ode, d_results, ctx->gil_counter, st);
     });
 }
 

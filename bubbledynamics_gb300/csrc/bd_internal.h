@@ -90,6 +90,9 @@ struct bd_context {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     int sm_count = 0;
     int64_t launches = 0;       // kernels of this library launched by the context
+    // work counter of the persistent Gilmore launches made by bd_gilmore_run_device
+    // (allocated with the context, freed with it)
+    unsigned long long* gil_counter = nullptr;
     // device blocks released by finished solves, reused by the next one of the same size
     std::multimap<size_t, void*> pool;
     size_t pool_bytes = 0;

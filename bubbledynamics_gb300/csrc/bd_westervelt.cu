@@ -505,7 +505,11 @@ static std::string tune_key(const WvSession& S) {
 }
 
 // Pick the fastest tile variant: a few steps of each on the (zero) initial
-// state, timed with events, then the state is cleared again.
+// state, timed with events, then the state is cleared again.  Every trial
+// restarts at step 0 (host ring index and device step counter), so the trials
+// read only the first kTuneSteps entries of the per-step tables, which hold
+// n_steps >= kTuneSteps entries whenever tuning runs.
+static const int kTuneWarm = 2, kTuneReps = 8, kTuneSteps = kTuneWarm + kTuneReps;
 static void autotune(WvSession& S) {
     const std::string key = tune_key(S);
     {
@@ -514,7 +518,7 @@ static void autotune(WvSession& S) {
         if (it != g_tuned.end()) { S.variant = it->second; return; }
     }
     cudaStream_t st = S.ctx->stream;
-    const int reps = 8;
+    if (S.p.n_steps < kTuneSteps) fail(BD_ERR_STATE, "tuning needs at least %d steps", kTuneSteps);
     std::vector<float> best_ms(kNumVariants, 1e30f);
     // two rounds over the variants, best time of each: the rounds are seconds
     // apart, so a clock change during one trial does not decide the choice
@@ -523,11 +527,13 @@ static void autotune(WvSession& S) {
             if (kVariants[v].zb == 0 && S.nz > 512) continue;
             if (kVariants[v].tma && !tma_eligible(S)) continue;
             if (!variant_ok(S, v)) continue;
-            issue_steps(S, v, S.step, 2, st);  // warm-up
-            S.step += 2;
+            BD_CUDA(cudaMemsetAsync(S.step_base.p, 0, sizeof(long long), st));
+            S.step = 0;
+            issue_steps(S, v, S.step, kTuneWarm, st);  // warm-up
+            S.step += kTuneWarm;
             BD_CUDA(cudaEventRecord(S.ctx->ev0, st));
-            issue_steps(S, v, S.step, reps, st);
-            S.step += reps;
+            issue_steps(S, v, S.step, kTuneReps, st);
+            S.step += kTuneReps;
             BD_CUDA(cudaEventRecord(S.ctx->ev1, st));
             BD_CUDA(cudaEventSynchronize(S.ctx->ev1));
             float ms = 0;

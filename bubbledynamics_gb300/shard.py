@@ -53,7 +53,10 @@ def allreduce_gradients(grad_phase, grad_amp, group=None):
     if not (dist.is_available() and dist.is_initialized()):
         return grad_phase, grad_amp
     t = torch.from_numpy(np.concatenate([grad_phase, grad_amp]).astype(np.float64))
+    if dist.get_backend(group) == "nccl":     # NCCL reduces device tensors only
+        t = t.to(torch.device("cuda", torch.cuda.current_device()))
     dist.all_reduce(t, op=dist.ReduceOp.SUM, group=group)
+    t = t.cpu()
     n = len(grad_phase)
     grad_phase[:] = t[:n].numpy()
     grad_amp[:] = t[n:].numpy()

@@ -358,11 +358,17 @@ bd_status bd_spiral_heat_run(bd_context* ctx, const bd_thermal* thermal, const d
  * thermal->material_map NULL (plane_material is honoured).
  *
  * The first call on a device looks up the address of that array (with the
- * device current); make that first call before any stream capture.  Every
- * call shares the array and leaves its contents behind, so two calls whose
- * work overlaps on the GPU (different streams, or different contexts on the
- * same device) race with each other; serialise them.  The call returns once
- * its work is enqueued on stream (NULL = the context's stream). */
+ * device current); make that first call before any stream capture.  The
+ * address stays valid for the life of the device's primary context: do not
+ * keep using the library after cudaDeviceReset.  Every call shares the array
+ * and leaves its contents behind, so two calls whose work overlaps on the GPU
+ * (different streams, or different contexts on the same device) race with
+ * each other; serialise them.  The call returns once its work is enqueued on
+ * stream (NULL = the context's stream).  shifts and thermal->plane_material
+ * are read by host-to-device copies enqueued on that stream: from pageable
+ * memory they are staged before the call returns; from page-locked memory the
+ * copy reads them when the stream reaches it, so keep them alive and unchanged
+ * until the stream has passed this call's work. */
 #define BD_NOALLOC_MAX_CELLS (1 << 21)
 #define BD_NOALLOC_MAX_STEPS (1 << 16)
 #define BD_NOALLOC_MAX_PLANES 4096
@@ -440,6 +446,11 @@ bd_status bd_gilmore_combos(int32_t n_fr, double f_min, double f_max, double* ou
 bd_status bd_gilmore_run(bd_context* ctx, const bd_gilmore_medium* medium, int64_t n,
                          const bd_bubble* bubbles, const bd_ode_params* ode,
                          bd_bubble_result* results, double* elapsed_ms);
+/* Device-pointer form: d_bubbles / d_results on the device, work enqueued on
+ * stream (NULL = the context's stream), returns once enqueued.  The persistent
+ * schedule's work counter belongs to the context, so two calls on one context
+ * whose work overlaps on the GPU (different streams) race on it: serialise
+ * them, or give each stream its own context. */
 bd_status bd_gilmore_run_device(bd_context* ctx, const bd_gilmore_medium* medium, int64_t n,
                                 const bd_bubble* d_bubbles, const bd_ode_params* ode,
                                 bd_bubble_result* d_results, void* stream);

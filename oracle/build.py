@@ -7,7 +7,8 @@
                                 extracted by line range into oracle/_ref/src/.
 
 Both outputs are git-ignored.  The extraction needs the reference tree (the
-REF_DIR environment variable or the default path below); where it is absent but
+BD_REFERENCE_DIR environment variable, else a directory named "reference"
+beside this repository); where it is absent but
 oracle/_ref/src/ already holds the extracted sections (a copy of this working
 tree on another machine), the library is compiled from those.
 """
@@ -17,7 +18,8 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_DIR = os.environ.get("BD_REFERENCE_DIR", "/root/reference")
+# the reference tree: BD_REFERENCE_DIR, else a "reference" directory beside this repository
+REF_DIR = os.environ.get("BD_REFERENCE_DIR", os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference"))
 REF_FILES = {
     "W": "Westervelt_relax_fft_Pressure_Energy.cu",
     "T": "Westervelt_Temperature_SquareSpiral.cu",

@@ -282,3 +282,20 @@ def test_kernel_launches_counted(ctx):
     p = presets.cfg1(32, 32, 48, 30, precision=abi.BD_F32)
     ctx.westervelt(p, want=("peak",))
     assert ctx.kernel_launches() - before >= 30
+
+
+def test_autotuned_short_run_matches_explicit_variant(ctx):
+    """A run large enough to be tuned (2^21 cells, 300 steps) whose step count
+    is below the tuner's total trial steps (10 per variant per round): every
+    trial restarts at step 0, so the trials stay inside the per-step source
+    tables, and the tuned solve equals the same problem run at the variant
+    the tuner chose."""
+    a = presets.cfg1(128, 128, 128, 300, precision=abi.BD_F32)
+    assert a.ncell >= 1 << 21
+    ra = ctx.westervelt(a, want=("p_final", "peak", "energy"))
+    b = presets.cfg1(128, 128, 128, 300, precision=abi.BD_F32)
+    b.params.tile_variant = int(ra["tile_variant"])
+    rb = ctx.westervelt(b, want=("p_final", "peak", "energy"))
+    assert np.abs(ra["peak"]).max() > 0
+    for k in ("p_final", "peak", "energy"):
+        np.testing.assert_array_equal(ra[k], rb[k], err_msg=k)

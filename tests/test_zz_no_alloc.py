@@ -24,13 +24,27 @@ def _problem():
     return prob, Q
 
 
-def test_noalloc_matches_allocating_entry_point_twice(ctx):
+def _even_spots(prob, n_steps):
+    """A spot trajectory of prob's grid with an even step count, so that the
+    last step writes the caller's own buffer (an odd count ends in the
+    scratch buffer and a copy back)."""
+    assert n_steps % 2 == 0
+    prob.set_spots(np.array([0, 2], np.int32), np.array([0, -1], np.int32),
+                   np.array([n_steps // 2, n_steps // 2], np.int64))
+    return prob
+
+
+@pytest.mark.parametrize("parity", ["odd", "even"])
+def test_noalloc_matches_allocating_entry_point_twice(ctx, parity):
     torch = pytest.importorskip("torch")
     lib = api.load()
     prob, Q = _problem()
+    if parity == "even":
+        prob = _even_spots(prob, 180)
     th = prob.thermal
     expected = ctx.heat(th, Q, prob.traj)
     sx, sy, _ = api.trajectory_shifts(prob.traj)
+    assert len(sx) % 2 == (1 if parity == "odd" else 0)
     shifts = np.ascontiguousarray(np.stack([sx, sy], axis=1).astype(np.int32).reshape(-1))
     T0, TD0 = prob.initial_fields()
     theta0 = (T0 - th.T_ref).astype(np.float32)
@@ -44,9 +58,12 @@ def test_noalloc_matches_allocating_entry_point_twice(ctx):
         d_Q = torch.from_numpy(Q.astype(np.float32)).cuda()
         d_dose = torch.from_numpy(dose0.copy()).cuda()
         torch.cuda.synchronize()
+        free_before = torch.cuda.mem_get_info()[0]
         api.check(lib.bd_heat_run_device_noalloc(ctx.h, C.byref(th), d_theta.data_ptr(), d_Q.data_ptr(),
                                                  d_dose.data_ptr(), shifts.ctypes.data, len(sx), None))
         torch.cuda.synchronize()
+        # the call allocated nothing on the device (the warm-up run above loaded the module)
+        assert torch.cuda.mem_get_info()[0] == free_before, call
         T = th.T_ref + d_theta.cpu().numpy().astype(np.float64)
         dd = d_dose.cpu().numpy().astype(np.float64)
         dose = dd[..., 0] + dd[..., 1]
