@@ -161,6 +161,7 @@ class Thermal(C.Structure):
         ("mat", ThermalMaterial * BD_MAX_MATERIALS),
         ("plane_material", vp), ("material_map", vp),
         ("T_start", vp), ("dose_start", vp),
+        ("plain_launches", i32), ("pad1", i32),
     ]
 
 

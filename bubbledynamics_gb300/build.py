@@ -1,7 +1,10 @@
-"""Build libbubbledyn.so (the C ABI of include/bubbledyn.h) for sm_103a.
+"""Build libbubbledyn.so (the C ABI of include/bubbledyn.h) for sm_103a, and
+the command-line drivers that call it.
 
 Each csrc/*.cu is compiled by nvcc in parallel into bubbledynamics_gb300/_build/
-and linked into bubbledynamics_gb300/lib/libbubbledyn.so (both git-ignored).
+and linked into bubbledynamics_gb300/lib/libbubbledyn.so; each cli/*.cpp is
+compiled by the host C++ compiler into bubbledynamics_gb300/bin/ and linked
+against that library (all git-ignored).
 """
 import concurrent.futures as cf
 import glob
@@ -16,6 +19,8 @@ OBJ = os.path.join(HERE, "_build")
 LIBDIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIBDIR, "libbubbledyn.so")
 INCLUDE = os.path.join(HERE, "..", "include")
+CLI_SRC = os.path.join(HERE, "cli")
+BINDIR = os.path.join(HERE, "bin")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
@@ -79,7 +84,34 @@ def build(force=False, verbose=False, extra=None):
         os.replace(tmp, LIB)
     if verbose:
         print(LIB)
+    build_cli()
     return LIB
+
+
+def cli_path(name):
+    return os.path.join(BINDIR, name)
+
+
+def build_cli():
+    """The command-line drivers (bd_westervelt, bd_spiral, bd_gilmore): host
+    C++ against the C ABI only, run-path set to the library's directory."""
+    os.makedirs(BINDIR, exist_ok=True)
+    cxx = os.environ.get("CXX", "g++")
+    hdrs = [os.path.join(CLI_SRC, "cli_common.h"), os.path.join(INCLUDE, "bubbledyn.h")]
+
+    def one(src):
+        exe = cli_path(os.path.basename(src)[:-4])
+        if _stale(exe, [src, LIB] + hdrs):
+            cmd = [cxx, "-O2", "-std=c++17", "-Wall", "-I", INCLUDE, src, "-o", exe, "-L", LIBDIR, "-lbubbledyn",
+                   "-Wl,-rpath,$ORIGIN/../lib"]
+            r = subprocess.run(cmd, capture_output=True, text=True)
+            if r.returncode != 0:
+                raise RuntimeError("C++ driver build failed for %s:\n%s\n%s" % (src, r.stdout, r.stderr))
+        return exe
+
+    srcs = sorted(glob.glob(os.path.join(CLI_SRC, "*.cpp")))
+    with cf.ThreadPoolExecutor(max(1, len(srcs))) as ex:
+        return list(ex.map(one, srcs))
 
 
 if __name__ == "__main__":

@@ -4,10 +4,12 @@
 // BD_F64: temperature in double, dose increment pow(4|2, T-43) dt exactly as
 //         T:99-102 (reference-faithful mode).
 // BD_F32: theta = T - T_ref in float (the per-step change of about 1e-4 K would
-//         be lost against 300 K in float), source Q in float, and the dose kept
-//         as a double-float pair (hi + lo, ~48-bit mantissa) updated with
-//         error-free FP32 sums, because FP64 arithmetic is the scarce unit on
-//         this GPU.  Traffic: theta read + write 8 B, Q 4 B, dose RMW 16 B.
+//         be lost against 300 K in float), source Q in float, the dose rate
+//         R^(T-43) in float and the dose itself accumulated in double (one
+//         FP64 add per cell and step).  Traffic: theta read + write 8 B, Q 4 B,
+//         dose RMW 16 B.
+// The allocation-free entry point keeps its dose as a double-float pair (hi,
+// lo) updated with error-free FP32 sums (its caller-owned buffer format).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -35,8 +37,8 @@ struct HeatArgs {
     const real* __restrict__ Tin;
     real* __restrict__ Tout;
     const real* __restrict__ Q;
-    double* __restrict__ TD;       // BD_F64 dose
-    float2* __restrict__ TDf;      // BD_F32 dose (hi, lo)
+    double* __restrict__ TD;       // dose [s] in double
+    float2* __restrict__ TDf;      // dose as (hi, lo) float pairs (allocation-free entry point; TD is then null)
     const int* __restrict__ plane_mat;
     const uint8_t* __restrict__ matmap;
     const int2* __restrict__ shifts;   // per step (sx, sy)
@@ -94,7 +96,8 @@ __global__ void heat_step_kernel(const HeatArgs<real> a, int koff) {
         } else {
             const float x = (float)tn + a.T_refm43;                    // T_C - 43
             const float inc = exp2f(x < 0.0f ? 2.0f * x : x) * (float)a.dt;
-            a.TDf[i] = df_add(a.TDf[i], inc);
+            if (a.TD) a.TD[i] = a.TD[i] + (double)inc;
+            else a.TDf[i] = df_add(a.TDf[i], inc);
         }
     };
     auto sxy_at = [&](int iz) {
@@ -163,8 +166,8 @@ __global__ void __launch_bounds__(128) heat_step4_kernel(const HeatArgs<float> a
             const int ixa = x0 + k - sh.x;
             q[k] = (qrow && ixa >= 0 && ixa < a.nx) ? __ldg(a.Q + (long long)iz * P + (long long)iya * NX + ixa) : 0.f;
         }
-        float4* dp = reinterpret_cast<float4*>(a.TDf + i);
-        float4 d01 = dp[0], d23 = dp[1];
+        double2* dp = reinterpret_cast<double2*>(a.TD + i);
+        double2 d01 = dp[0], d23 = dp[1];
         int mats[4];
         if (a.matmap) {
             const uchar4 mm = *reinterpret_cast<const uchar4*>(a.matmap + i);
@@ -177,7 +180,7 @@ __global__ void __launch_bounds__(128) heat_step4_kernel(const HeatArgs<float> a
         const float xl[4] = {L.w, tc.x, tc.y, tc.z}, xr[4] = {tc.y, tc.z, tc.w, R.x};
         const float su[4] = {yu.x, yu.y, yu.z, yu.w}, sd[4] = {yd.x, yd.y, yd.z, yd.w};
         const float zu[4] = {tp.x, tp.y, tp.z, tp.w}, zd[4] = {tm.x, tm.y, tm.z, tm.w};
-        float dh[4] = {d01.x, d01.z, d23.x, d23.z}, dl[4] = {d01.y, d01.w, d23.y, d23.w};
+        double dose[4] = {d01.x, d01.y, d23.x, d23.y};
         float tn[4];
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
@@ -188,15 +191,13 @@ __global__ void __launch_bounds__(128) heat_step4_kernel(const HeatArgs<float> a
             tn[k] = upd[k] ? t : cv[k];
             if (upd[k]) {
                 const float x = t + a.T_refm43;                   // T_C - 43
-                const float inc = exp2f(x < 0.0f ? 2.0f * x : x) * a.dt;
-                const float2 r = df_add(make_float2(dh[k], dl[k]), inc);
-                dh[k] = r.x;
-                dl[k] = r.y;
+                const float inc = exp2f(x < 0.0f ? 2.0f * x : x) * a.dt;   // T:99-102
+                dose[k] = dose[k] + (double)inc;
             }
         }
         *reinterpret_cast<float4*>(a.Tout + i) = make_float4(tn[0], tn[1], tn[2], tn[3]);
-        dp[0] = make_float4(dh[0], dl[0], dh[1], dl[1]);
-        dp[1] = make_float4(dh[2], dl[2], dh[3], dl[3]);
+        dp[0] = make_double2(dose[0], dose[1]);
+        dp[1] = make_double2(dose[2], dose[3]);
         tm = tc;
         tc = tp;
     }
@@ -381,17 +382,14 @@ bd_status bd_spiral_heat_run(bd_context* ctx, const bd_thermal* th, const double
             BD_CUDA(cudaMemcpy(TDd.p, TD0.data(), n * 8, cudaMemcpyHostToDevice));
         } else {
             std::vector<float> tf(n), qf(n);
-            std::vector<float2> df(n);
             for (long long i = 0; i < n; ++i) {
                 tf[i] = (float)(T0[i] - T_ref);
                 qf[i] = (float)Q[i];
-                const float hi = (float)TD0[i];
-                df[i] = make_float2(hi, (float)(TD0[i] - (double)hi));
             }
             BD_CUDA(cudaMemcpy(Ta.p, tf.data(), n * 4, cudaMemcpyHostToDevice));
             BD_CUDA(cudaMemcpy(Tb.p, tf.data(), n * 4, cudaMemcpyHostToDevice));
             BD_CUDA(cudaMemcpy(Qd.p, qf.data(), n * 4, cudaMemcpyHostToDevice));
-            BD_CUDA(cudaMemcpy(TDd.p, df.data(), n * 8, cudaMemcpyHostToDevice));
+            BD_CUDA(cudaMemcpy(TDd.p, TD0.data(), n * 8, cudaMemcpyHostToDevice));
         }
         if (th->plane_material) {
             pm.alloc(ctx, nz * 4);
@@ -459,7 +457,7 @@ bd_status bd_spiral_heat_run(bd_context* ctx, const bd_thermal* th, const double
             a.Tout = (a_to_b ? Tb : Ta).template as<RR>();
             a.Q = Qd.template as<RR>();
             a.TD = TDd.template as<double>();
-            a.TDf = TDd.template as<float2>();
+            a.TDf = nullptr;
             a.plane_mat = th->plane_material ? pm.template as<int>() : nullptr;
             a.matmap = th->material_map ? mm.template as<uint8_t>() : nullptr;
             a.shifts = shd.template as<int2>();
@@ -468,31 +466,71 @@ bd_status bd_spiral_heat_run(bd_context* ctx, const bd_thermal* th, const double
             a.T_ref = T_ref;
             a.T_refm43 = (float)(T_ref - 273.15 - 43.0);
         };
+        // the reference toggles use_p each step (T:391); with Tin/Tout swapped per
+        // step, after an even number of steps the latest field is Ta.  Steps go
+        // out in chunks of CH: the kernels read their step as the device counter
+        // plus their offset in the chunk, and one advance kernel moves the counter,
+        // so a chunk depends only on the parity of its first step and one captured
+        // CUDA graph per parity serves every full chunk.
+        const int CH = 64;
+        auto issue = [&](cudaStream_t st, int64_t s0, int cnt) {
+            for (int k = 0; k < cnt; ++k) {
+                const bool a_to_b = ((s0 + k) % 2) == 0;
+                if (f64) {
+                    HeatArgs<double> a = margs.second;
+                    fill(a, a_to_b, 0.0);
+                    heat_step_kernel<double><<<grid, block, 0, st>>>(a, k);
+                } else {
+                    HeatArgs<float> a = margs.first;
+                    fill(a, a_to_b, 0.0f);
+                    if (vec4) heat_step4_kernel<<<grid4, block4, 0, st>>>(a, k);
+                    else heat_step_kernel<float><<<grid, block, 0, st>>>(a, k);
+                }
+                BD_LAUNCHED(ctx);
+            }
+            heat_advance_kernel<<<1, 32, 0, st>>>(sb.as<long long>(), cnt);
+            BD_LAUNCHED(ctx);
+        };
+        struct Graphs {
+            cudaGraphExec_t g[2] = {nullptr, nullptr};
+            ~Graphs() { for (auto e : g) if (e) cudaGraphExecDestroy(e); }
+        } graphs;
+        auto chunk_graph = [&](int parity) {
+            if (graphs.g[parity]) return graphs.g[parity];
+            cudaStream_t cs;
+            BD_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+            cudaGraph_t g = nullptr;
+            const int64_t before = ctx->launches;
+            BD_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+            try {
+                issue(cs, parity, CH);
+            } catch (...) {
+                cudaStreamEndCapture(cs, &g);
+                if (g) cudaGraphDestroy(g);
+                cudaStreamDestroy(cs);
+                throw;
+            }
+            BD_CUDA(cudaStreamEndCapture(cs, &g));
+            ctx->launches = before;   // captured, not launched
+            const cudaError_t e = cudaGraphInstantiate(&graphs.g[parity], g, 0);
+            cudaGraphDestroy(g);
+            cudaStreamDestroy(cs);
+            BD_CUDA(e);
+            return graphs.g[parity];
+        };
+        const bool use_graph = th->plain_launches == 0;
         BD_CUDA(cudaEventRecord(ctx->ev0, s));
         int64_t done = 0;
         size_t isnap = 0;
-        // the reference toggles use_p each step (T:391); with Tin/Tout swapped per
-        // step, after an even number of steps the latest field is Ta
         auto run_steps = [&](int64_t from, int64_t to) {
-            const int CH = 64;
             for (int64_t s0 = from; s0 < to; s0 += CH) {
                 const int cnt = (int)std::min<int64_t>(CH, to - s0);
-                for (int k = 0; k < cnt; ++k) {
-                    const bool a_to_b = ((s0 + k) % 2) == 0;
-                    if (f64) {
-                        HeatArgs<double> a = margs.second;
-                        fill(a, a_to_b, 0.0);
-                        heat_step_kernel<double><<<grid, block, 0, s>>>(a, k);
-                    } else {
-                        HeatArgs<float> a = margs.first;
-                        fill(a, a_to_b, 0.0f);
-                        if (vec4) heat_step4_kernel<<<grid4, block4, 0, s>>>(a, k);
-                        else heat_step_kernel<float><<<grid, block, 0, s>>>(a, k);
-                    }
-                    BD_LAUNCHED(ctx);
+                if (use_graph && cnt == CH) {
+                    BD_CUDA(cudaGraphLaunch(chunk_graph((int)(s0 % 2)), s));
+                    ctx->launches += CH + 1;
+                } else {
+                    issue(s, s0, cnt);
                 }
-                heat_advance_kernel<<<1, 32, 0, s>>>(sb.as<long long>(), cnt);
-                BD_LAUNCHED(ctx);
             }
         };
         double snap_ms = 0.0;
@@ -516,14 +554,7 @@ bd_status bd_spiral_heat_run(bd_context* ctx, const bd_thermal* th, const double
         (void)snap_ms;
         const PoolBuf& latest = (nsteps % 2 == 0) ? Ta : Tb;
         if (out->T_final) copy_T(latest, static_cast<double*>(out->T_final));
-        if (out->dose) {
-            if (f64) BD_CUDA(cudaMemcpy(out->dose, TDd.p, n * 8, cudaMemcpyDeviceToHost));
-            else {
-                std::vector<float2> df(n);
-                BD_CUDA(cudaMemcpy(df.data(), TDd.p, n * 8, cudaMemcpyDeviceToHost));
-                for (long long i = 0; i < n; ++i) out->dose[i] = (double)df[i].x + (double)df[i].y;
-            }
-        }
+        if (out->dose) BD_CUDA(cudaMemcpy(out->dose, TDd.p, n * 8, cudaMemcpyDeviceToHost));
         out->elapsed_ms = ms;
         out->steps_done = nsteps;
     });
@@ -566,6 +597,7 @@ bd_status bd_heat_run_device_noalloc(bd_context* ctx, const bd_thermal* th, floa
         heat_materials<float>(th, th->T_ref, a.mat);
         a.nx = nx; a.ny = ny; a.nz = nz; a.zb = 32; a.plane = (long long)nx * ny;
         a.Q = d_Q;
+        a.TD = nullptr;
         a.TDf = reinterpret_cast<float2*>(d_dose);
         a.plane_mat = th->plane_material ? sc.planemat : nullptr;
         a.matmap = nullptr;

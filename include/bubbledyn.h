@@ -286,6 +286,10 @@ typedef struct bd_thermal {
     const double* T_start;          /* optional nx*ny*nz initial temperature [K] (NULL: mat[].T_init) */
     const double* dose_start;       /* optional nx*ny*nz initial dose [s] (NULL: dose_init rule);
                                        with both, a run continues where an earlier one ended */
+    int32_t plain_launches;         /* 0: the step loop replays one captured CUDA graph per 64 steps
+                                       (replaces T's launch + cudaDeviceSynchronize per step, T:345-392);
+                                       1: one launch per step */
+    int32_t pad1;
 } bd_thermal;
 
 typedef enum bd_trajectory_kind {
