@@ -63,6 +63,11 @@ def load(path=None):
     _sig(L, "bd_westervelt_finish", [P, P])
     _sig(L, "bd_westervelt_end", [P])
     _sig(L, "bd_westervelt_last_ms", [P, C.POINTER(C.c_double)])
+    _sig(L, "bd_westervelt_slab_begin", [P, P, P, P, P, C.c_int32, C.c_int32, C.POINTER(P)])
+    _sig(L, "bd_westervelt_halo_bytes", [P, C.POINTER(C.c_size_t)])
+    _sig(L, "bd_westervelt_halo_copy", [P, C.c_int32, C.c_int32, P, P])
+    _sig(L, "bd_halo_exchange", [P, P])
+    _sig(L, "bd_westervelt_run_slabs", [P, P, P, P, P, C.c_int32, P])
     _sig(L, "bd_checkpoint_size", [P, C.POINTER(C.c_size_t)])
     _sig(L, "bd_checkpoint_save", [P, P, C.c_size_t])
     _sig(L, "bd_checkpoint_load", [P, P, C.c_size_t])
@@ -254,6 +259,19 @@ class Context:
     def westervelt_session(self, prob: WesterveltProblem):
         return WesterveltSession(self, prob)
 
+    def westervelt_slabs(self, prob: WesterveltProblem, n_slabs, want=("p_final", "peak", "energy", "Q", "dft")):
+        """The solve as n_slabs z slabs on this device with the ghost planes
+        exchanged after every step (bd_westervelt_run_slabs): the same outputs
+        as westervelt(), bit for bit."""
+        out, res = self._outputs(prob, want)
+        check(self.L.bd_westervelt_run_slabs(self.h, C.byref(prob.grid), C.byref(prob.medium), C.byref(prob.source),
+                                             C.byref(prob.params), int(n_slabs), C.byref(out)))
+        return self._shape(prob, res, out)
+
+    def westervelt_slab(self, prob: WesterveltProblem, z_begin, z_end):
+        """Session over the planes [z_begin, z_end) of prob (bd_westervelt_slab_begin)."""
+        return WesterveltSession(self, prob, slab=(int(z_begin), int(z_end)))
+
     def westervelt_adjoint(self, prob: WesterveltProblem, loss):
         """Loss of `loss` (abi.FocalLoss) and its gradient w.r.t. the element
         phases and amplitudes of prob's BD_SRC_ARRAY source
@@ -325,14 +343,35 @@ class Context:
 class WesterveltSession:
     """bd_westervelt_begin / advance / checkpoint / finish / end."""
 
-    def __init__(self, ctx: Context, prob: WesterveltProblem):
+    def __init__(self, ctx: Context, prob: WesterveltProblem, slab=None):
         self.ctx = ctx
         self.prob = prob
         self.L = ctx.L
+        self.slab = slab
         h = P()
-        check(self.L.bd_westervelt_begin(ctx.h, C.byref(prob.grid), C.byref(prob.medium), C.byref(prob.source),
-                                         C.byref(prob.params), C.byref(h)))
+        if slab is None:
+            check(self.L.bd_westervelt_begin(ctx.h, C.byref(prob.grid), C.byref(prob.medium), C.byref(prob.source),
+                                             C.byref(prob.params), C.byref(h)))
+        else:
+            check(self.L.bd_westervelt_slab_begin(ctx.h, C.byref(prob.grid), C.byref(prob.medium),
+                                                  C.byref(prob.source), C.byref(prob.params), slab[0], slab[1],
+                                                  C.byref(h)))
         self.h = h
+
+    # -- z slabs: halo messages of the newest pressure level
+    def halo_bytes(self):
+        n = C.c_size_t(0)
+        check(self.L.bd_westervelt_halo_bytes(self.h, C.byref(n)))
+        return n.value
+
+    def halo_copy(self, side, to_ghost, d_ptr, stream=None):
+        """side 0 / 1 = low / high z face; to_ghost 0 packs the owned planes into
+        the device buffer at d_ptr, 1 unpacks it into the ghost planes."""
+        check(self.L.bd_westervelt_halo_copy(self.h, int(side), int(to_ghost), d_ptr, stream))
+
+    def exchange_with(self, upper):
+        """Same-device halo exchange with the neighbouring slab above (bd_halo_exchange)."""
+        check(self.L.bd_halo_exchange(self.h, upper.h))
 
     def advance(self, n):
         check(self.L.bd_westervelt_advance(self.h, int(n)))
@@ -359,9 +398,38 @@ class WesterveltSession:
         check(self.L.bd_checkpoint_load(self.h, _ptr(blob), blob.size))
 
     def finish(self, want=("p_final", "peak", "energy", "Q", "dft")):
+        if self.slab is not None:
+            return self._finish_slab(want)
         out, res = Context._outputs(self.prob, want)
         check(self.L.bd_westervelt_finish(self.h, C.byref(out)))
         return Context._shape(self.prob, res, out)
+
+    def _finish_slab(self, want):
+        """The owned planes of a slab session, shaped (z_end - z_begin, ny, nx)."""
+        zb, ze = self.slab
+        g, p = self.prob.grid, self.prob.params
+        dt = self.prob.dtype
+        plane = g.nx * g.ny
+        out = abi.WesterveltOutputs()
+        res = {}
+        for k in ("p_final", "peak", "energy"):
+            if k in want:
+                res[k] = np.zeros((ze - zb) * plane, dt)
+                setattr(out, k, _ptr(res[k]))
+        if "dft" in want and p.n_dft > 0:
+            nz = max(0, min(ze, p.dft_z_hi) - max(zb, p.dft_z_lo))
+            res["dft_re"] = np.zeros(p.n_dft * plane * nz, dt)
+            res["dft_im"] = np.zeros(p.n_dft * plane * nz, dt)
+            out.dft_re, out.dft_im = _ptr(res["dft_re"]), _ptr(res["dft_im"])
+        if "Q" in want and p.q_mode == abi.BD_Q_REFERENCE:
+            res["Q"] = np.zeros((ze - zb) * plane, np.float64)
+            out.Q = _ptr(res["Q"])
+        check(self.L.bd_westervelt_finish(self.h, C.byref(out)))
+        for k in ("p_final", "peak", "energy", "Q"):
+            if k in res:
+                res[k] = res[k].reshape(ze - zb, g.ny, g.nx)
+        res["steps_done"] = out.steps_done
+        return res
 
     def close(self):
         if self.h:

@@ -17,6 +17,7 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <tuple>
@@ -98,6 +99,15 @@ struct WvSession {
     std::vector<bd_material> mats;
     int n_materials = 0;
     bool has_cmap = false, has_matmap = false, has_planemat = false;
+    // z slab of a larger grid (slab sessions only): local plane 0 is global plane
+    // zoff, planes [own0, own1) are owned, the 3 planes beyond an internal face
+    // are ghost copies of the neighbour's planes (refreshed by the halo exchange)
+    bool slab = false;
+    int zoff = 0, nz_glob = 0, own0 = 0, own1 = 0;
+    int glob_face_zm = BD_FACE_OPEN, glob_face_zp = BD_FACE_OPEN;
+    // DFT output layout: this session's planes sit at cell offset dft_glob_off of
+    // frequency blocks of dft_glob_cells cells (a whole grid: dcells and 0)
+    long long dft_glob_cells = 0, dft_glob_off = 0;
 
     ~WvSession() {
         if (graph) cudaGraphExecDestroy(graph);
@@ -105,6 +115,11 @@ struct WvSession {
 };
 
 static inline int head_of(int64_t s) { return (int)((4 * (s % 5)) % 5); }
+
+// Internal z face of a slab session (never set by callers): the 3 planes beyond
+// it are ghost planes, not updated by the step and not damped or Mur-treated.
+static const int kFaceHalo = 3;
+static const int kHalo = 3;   // ghost planes: the 6th-order stencil reaches iz +- 3 (W:169-174)
 
 template <class real>
 static WvArgs<real> make_args(WvSession& S, int64_t s) {
@@ -141,10 +156,17 @@ static WvArgs<real> make_args(WvSession& S, int64_t s) {
     a.yhi = a.mur_yp ? S.ny - 1 - a.L : S.ny - 1;
     a.zlo = a.Lzm;
     a.zhi = a.mur_zp ? S.nz - 1 - a.L : S.nz - 1;
+    if (g.face[4] == kFaceHalo) a.zlo = std::max(a.zlo, kHalo);
+    if (g.face[5] == kFaceHalo) a.zhi = std::min(a.zhi, S.nz - 1 - kHalo);
     if (g.sponge_cells > 0) { a.wx = S.wx.as<real>(); a.wy = S.wy.as<real>(); a.wz = S.wz.as<real>(); }
     a.dt = (real)g.dt;
-    a.kxy180 = (real)(g.dt * g.dt / (g.dx * g.dx) / 180.0);
-    a.kz180 = (real)(g.dt * g.dt / (g.dz * g.dz) / 180.0);
+    {
+        const double kxy = g.dt * g.dt / (g.dx * g.dx) / 180.0, kz = g.dt * g.dt / (g.dz * g.dz) / 180.0;
+        a.kxy180 = (real)kxy;
+        a.kz180 = (real)kz;
+        a.kxy180l = (real)(kxy - (double)a.kxy180);
+        a.kz180l = (real)(kz - (double)a.kz180);
+    }
     a.dt2 = (real)(g.dt * g.dt);
     a.dtdx = (real)(g.dt / g.dx);
     a.dtdz = (real)(g.dt / g.dz);
@@ -600,6 +622,12 @@ static void setup(WvSession& S, bd_context* ctx, const bd_grid* g, const bd_medi
     if (g->face[1] == BD_FACE_MIRROR || g->face[3] == BD_FACE_MIRROR || g->face[4] == BD_FACE_MIRROR ||
         g->face[5] == BD_FACE_MIRROR)
         fail(BD_ERR_INVALID_ARG, "mirror planes exist only at x = 0 and y = 0");
+    for (int f = 0; f < 6; ++f) {
+        const bool halo_ok = S.slab && f >= 4 && g->face[f] == kFaceHalo;
+        if (!halo_ok && (g->face[f] < BD_FACE_OPEN || g->face[f] > BD_FACE_MIRROR))
+            fail(BD_ERR_INVALID_ARG, "face %d: unknown boundary kind %d", f, g->face[f]);
+    }
+    if (!S.slab) { S.zoff = 0; S.nz_glob = g->nz; S.own0 = 0; S.own1 = g->nz; }
     S.any_mur = false;
     for (int f = 0; f < 6; ++f) if (g->face[f] == BD_FACE_MUR) S.any_mur = true;
     if (S.any_mur && (g->mur_layers < 1 || g->mur_layers > 8)) fail(BD_ERR_INVALID_ARG, "mur_layers must be 1..8");
@@ -631,6 +659,8 @@ static void setup(WvSession& S, bd_context* ctx, const bd_grid* g, const bd_medi
         if (S.dz_hi <= S.dz_lo || p->dft_len <= 0) S.n_dft = 0;
     }
     S.dcells = S.n_dft > 0 ? (long long)(S.dz_hi - S.dz_lo) * S.plane : 0;
+    if (!S.slab) { S.dft_glob_cells = S.dcells; S.dft_glob_off = 0; }
+    if (S.slab) S.pdl = false;   // the halo copies between steps are not kernels: plain stream order
     S.chunk = p->graph_chunk > 0 ? ((p->graph_chunk + 9) / 10) * 10 : 50;
 
     BD_CUDA(cudaSetDevice(ctx->device));
@@ -691,7 +721,13 @@ static void setup(WvSession& S, bd_context* ctx, const bd_grid* g, const bd_medi
         if (g->sponge_cells > 0) {
             up(S.wx, prof(S.nx, g->face[0], g->face[1]));
             up(S.wy, prof(S.ny, g->face[2], g->face[3]));
-            up(S.wz, prof(S.nz, g->face[4], g->face[5]));
+            if (S.slab) {
+                // the whole grid's z profile, restricted to this slab's planes
+                const std::vector<double> wz = prof(S.nz_glob, S.glob_face_zm, S.glob_face_zp);
+                up(S.wz, std::vector<double>(wz.begin() + S.zoff, wz.begin() + S.zoff + S.nz));
+            } else {
+                up(S.wz, prof(S.nz, g->face[4], g->face[5]));
+            }
         }
     }
     // source plane (W:62-85): amplitude, var, delay per plane cell
@@ -780,6 +816,104 @@ static void setup(WvSession& S, bd_context* ctx, const bd_grid* g, const bd_medi
     }
 }
 
+// ---------------------------------------------------------------- z slabs
+// Global planes of the slab that owns [zb, ze) of grid g: the owned planes plus
+// kHalo ghost planes beyond each internal face.
+static void slab_extent(const bd_grid* g, int zb, int ze, int& lo, int& hi) {
+    lo = zb > 0 ? zb - kHalo : 0;
+    hi = ze < g->nz ? ze + kHalo : g->nz;
+}
+
+// A session for the planes [zb, ze) of the whole problem (g, m, src, p): the
+// grid, medium maps, source plane, sponge profile, DFT planes and power split
+// are those of the whole problem restricted to the slab, so that with the ghost
+// planes refreshed after every step (halo_exchange) the owned planes evolve
+// bit for bit as in a single session over the whole grid.
+static void setup_slab(WvSession& S, bd_context* ctx, const bd_grid* g, const bd_medium* m, const bd_source* src,
+                       const bd_westervelt_params* p, int zb, int ze) {
+    if (!ctx || !g || !m || !p) fail(BD_ERR_INVALID_ARG, "null argument");
+    if (!(0 <= zb && zb < ze && ze <= g->nz)) fail(BD_ERR_INVALID_ARG, "slab [%d, %d) outside 0..%d", zb, ze, g->nz);
+    if (ze - zb < 8) fail(BD_ERR_INVALID_ARG, "a slab must own at least 8 planes (%d)", ze - zb);
+    for (int f = 4; f < 6; ++f)
+        if (g->face[f] == kFaceHalo) fail(BD_ERR_INVALID_ARG, "face %d: unknown boundary kind", f);
+    // Mur layers at the grid's z faces stay inside the end slabs
+    const bool src_on = src && src->kind != BD_SRC_NONE;
+    const int Lzm = g->face[4] == BD_FACE_MUR ? (src_on ? src->plane_iz : g->mur_layers) : 0;
+    const int Lzp = g->face[5] == BD_FACE_MUR ? g->mur_layers : 0;
+    if ((zb > 0 && zb - kHalo < Lzm + 1) || (ze < g->nz && ze + kHalo > g->nz - Lzp - 1))
+        fail(BD_ERR_INVALID_ARG, "slab [%d, %d) cuts into the Mur layers of the z faces", zb, ze);
+    int lo = 0, hi = 0;
+    slab_extent(g, zb, ze, lo, hi);
+    const long long plane = (long long)g->nx * g->ny;
+    bd_grid gl = *g;
+    gl.nz = hi - lo;
+    gl.z0 = g->z0 + lo * g->dz;
+    if (zb > 0) gl.face[4] = kFaceHalo;
+    if (ze < g->nz) gl.face[5] = kFaceHalo;
+    bd_medium ml = *m;
+    if (m->plane_material) ml.plane_material = m->plane_material + lo;
+    if (m->material_map) ml.material_map = m->material_map + (size_t)lo * plane;
+    if (m->c_map) ml.c_map = m->c_map + (size_t)lo * plane;
+    bd_source sl;
+    if (src) {
+        sl = *src;
+        if (src_on) {
+            sl.plane_iz = src->plane_iz - lo;
+            if (sl.plane_iz < 0 || sl.plane_iz >= gl.nz) sl.kind = BD_SRC_NONE;
+        }
+    }
+    bd_westervelt_params pl = *p;
+    if (p->n_dft > 0) {
+        pl.dft_z_lo = std::max(p->dft_z_lo, zb) - lo;
+        pl.dft_z_hi = std::min(p->dft_z_hi, ze) - lo;
+    }
+    pl.q_iz_split = p->q_iz_split - lo;
+    S.slab = true;
+    S.zoff = lo;
+    S.nz_glob = g->nz;
+    S.own0 = zb - lo;
+    S.own1 = ze - lo;
+    S.glob_face_zm = g->face[4];
+    S.glob_face_zp = g->face[5];
+    setup(S, ctx, &gl, &ml, src ? &sl : nullptr, &pl);
+    // DFT planes of this slab inside the whole problem's DFT planes
+    if (S.n_dft > 0) {
+        const int glo = std::max(0, p->dft_z_lo), ghi = std::min(g->nz, p->dft_z_hi);
+        S.dft_glob_cells = (long long)(ghi - glo) * plane;
+        S.dft_glob_off = (long long)(S.zoff + S.dz_lo - glo) * plane;
+    }
+}
+
+// Refresh the ghost planes of two neighbouring slabs on the same device: the
+// lower slab's top kHalo owned planes of the newest level p^n go to the upper
+// slab's low ghost planes and the upper slab's bottom kHalo owned planes to the
+// lower slab's high ghost planes (replaces nothing in W, which runs one grid;
+// the exchange a multi-GPU run makes over NCCL or peer copies).
+static void halo_exchange(WvSession& lo, WvSession& hi, cudaStream_t st) {
+    if (!lo.slab || !hi.slab || lo.zoff + lo.own1 != hi.zoff + hi.own0 || lo.nx != hi.nx || lo.ny != hi.ny ||
+        lo.prec != hi.prec || lo.step != hi.step || lo.g.face[5] != kFaceHalo || hi.g.face[4] != kFaceHalo)
+        fail(BD_ERR_STATE, "halo exchange between sessions that are not neighbouring slabs at the same step");
+    const size_t pb = (size_t)lo.plane * lo.esz;
+    char* L = static_cast<char*>(lo.P[head_of(lo.step)].p);
+    char* H = static_cast<char*>(hi.P[head_of(hi.step)].p);
+    BD_CUDA(cudaMemcpyAsync(H, L + (size_t)(lo.own1 - kHalo) * pb, kHalo * pb, cudaMemcpyDeviceToDevice, st));
+    BD_CUDA(cudaMemcpyAsync(L + (size_t)lo.own1 * pb, H + (size_t)hi.own0 * pb, kHalo * pb, cudaMemcpyDeviceToDevice, st));
+}
+
+// Copy between the newest level's planes at one internal face and a caller's
+// device buffer of kHalo planes: to_ghost = 0 reads the owned planes next to
+// the face (what the neighbour needs), 1 writes the ghost planes beyond it.
+static void halo_copy(WvSession& S, int side, int to_ghost, void* buf, cudaStream_t st) {
+    if (!S.slab || (side != 0 && side != 1)) fail(BD_ERR_INVALID_ARG, "halo copy needs a slab session and side 0 or 1");
+    if (S.g.face[4 + side] != kFaceHalo) fail(BD_ERR_INVALID_ARG, "side %d of this slab is a face of the grid", side);
+    const size_t pb = (size_t)S.plane * S.esz;
+    char* P = static_cast<char*>(S.P[head_of(S.step)].p);
+    const int first = side == 0 ? (to_ghost ? S.own0 - kHalo : S.own0) : (to_ghost ? S.own1 : S.own1 - kHalo);
+    char* planes = P + (size_t)first * pb;
+    if (to_ghost) BD_CUDA(cudaMemcpyAsync(planes, buf, kHalo * pb, cudaMemcpyDeviceToDevice, st));
+    else BD_CUDA(cudaMemcpyAsync(buf, planes, kHalo * pb, cudaMemcpyDeviceToDevice, st));
+}
+
 // Acoustic power of W:242-265 (water planes) and W:324-345 (harmonics), in double.
 template <class real>
 __global__ void wv_q_kernel(const real* __restrict__ energy, const real* __restrict__ dre, const real* __restrict__ dim,
@@ -816,13 +950,22 @@ __global__ void wv_q_kernel(const real* __restrict__ energy, const real* __restr
 static void finish(WvSession& S, bd_westervelt_outputs* o) {
     cudaStream_t st = S.ctx->stream;
     BD_CUDA(cudaStreamSynchronize(st));
-    const size_t bytes = S.ncell * S.esz;
+    // owned planes only (a whole grid owns every plane)
+    const size_t off = (size_t)S.own0 * S.plane * S.esz;
+    const size_t bytes = (size_t)(S.own1 - S.own0) * S.plane * S.esz;
     const int h = head_of(S.step);
-    if (o->p_final) BD_CUDA(cudaMemcpy(o->p_final, S.P[h].p, bytes, cudaMemcpyDeviceToHost));
-    if (o->peak) BD_CUDA(cudaMemcpy(o->peak, S.peak.p, bytes, cudaMemcpyDeviceToHost));
-    if (o->energy) BD_CUDA(cudaMemcpy(o->energy, S.energy.p, bytes, cudaMemcpyDeviceToHost));
-    if (S.n_dft > 0 && o->dft_re) BD_CUDA(cudaMemcpy(o->dft_re, S.dre.p, S.dre.bytes, cudaMemcpyDeviceToHost));
-    if (S.n_dft > 0 && o->dft_im) BD_CUDA(cudaMemcpy(o->dft_im, S.dim.p, S.dim.bytes, cudaMemcpyDeviceToHost));
+    auto at = [&](const PoolBuf& b) { return static_cast<const char*>(b.p) + off; };
+    if (o->p_final) BD_CUDA(cudaMemcpy(o->p_final, at(S.P[h]), bytes, cudaMemcpyDeviceToHost));
+    if (o->peak) BD_CUDA(cudaMemcpy(o->peak, at(S.peak), bytes, cudaMemcpyDeviceToHost));
+    if (o->energy) BD_CUDA(cudaMemcpy(o->energy, at(S.energy), bytes, cudaMemcpyDeviceToHost));
+    for (int j = 0; j < S.n_dft; ++j) {
+        const size_t src = (size_t)j * S.dcells * S.esz, dst = ((size_t)j * S.dft_glob_cells + S.dft_glob_off) * S.esz;
+        const size_t nb = (size_t)S.dcells * S.esz;
+        if (o->dft_re) BD_CUDA(cudaMemcpy(static_cast<char*>(o->dft_re) + dst, static_cast<const char*>(S.dre.p) + src, nb,
+                                          cudaMemcpyDeviceToHost));
+        if (o->dft_im) BD_CUDA(cudaMemcpy(static_cast<char*>(o->dft_im) + dst, static_cast<const char*>(S.dim.p) + src, nb,
+                                          cudaMemcpyDeviceToHost));
+    }
     if (o->Q && S.p.q_mode == BD_Q_REFERENCE) {
         S.Qd.alloc(S.ctx, S.ncell * 8);
         PoolBuf mats;
@@ -845,7 +988,8 @@ static void finish(WvSession& S, bd_westervelt_outputs* o) {
                                                         S.p.q_n_harm, S.n_dft, S.dz_lo, S.dz_hi, S.p.q_freq,
                                                         (double)S.p.dft_len, S.Qd.as<double>());
         BD_LAUNCHED(S.ctx);
-        BD_CUDA(cudaMemcpyAsync(o->Q, S.Qd.p, S.ncell * 8, cudaMemcpyDeviceToHost, st));
+        BD_CUDA(cudaMemcpyAsync(o->Q, S.Qd.as<double>() + (size_t)S.own0 * S.plane,
+                                (size_t)(S.own1 - S.own0) * S.plane * 8, cudaMemcpyDeviceToHost, st));
         BD_CUDA(cudaStreamSynchronize(st));
     }
     o->steps_done = S.step;
@@ -1378,6 +1522,100 @@ bd_status bd_westervelt_adjoint(bd_context* ctx, const bd_grid* grid, const bd_m
         setup(w.S, ctx, grid, medium, source, &p);
         if (w.S.prec == BD_F32) adjoint_solve<float>(w.S, loss, loss_out, grad_phase, grad_amp, timings_ms);
         else adjoint_solve<double>(w.S, loss, loss_out, grad_phase, grad_amp, timings_ms);
+    });
+}
+
+bd_status bd_westervelt_slab_begin(bd_context* ctx, const bd_grid* grid, const bd_medium* medium,
+                                   const bd_source* source, const bd_westervelt_params* params, int32_t z_begin,
+                                   int32_t z_end, bd_westervelt** out) {
+    return guard([&] {
+        if (!out) fail(BD_ERR_INVALID_ARG, "null output");
+        *out = nullptr;
+        ctx_check(ctx);
+        auto* w = new bd_westervelt();
+        try {
+            setup_slab(w->S, ctx, grid, medium, source, params, z_begin, z_end);
+        } catch (...) {
+            delete w;
+            throw;
+        }
+        *out = w;
+    });
+}
+
+bd_status bd_westervelt_halo_bytes(bd_westervelt* w, size_t* bytes) {
+    return guard([&] {
+        if (!w || !bytes) fail(BD_ERR_INVALID_ARG, "null argument");
+        if (!w->S.slab) fail(BD_ERR_INVALID_ARG, "not a slab session");
+        *bytes = (size_t)kHalo * w->S.plane * w->S.esz;
+    });
+}
+
+bd_status bd_westervelt_halo_copy(bd_westervelt* w, int32_t side, int32_t to_ghost, void* d_buf, void* stream) {
+    return guard([&] {
+        if (!w || !d_buf) fail(BD_ERR_INVALID_ARG, "null argument");
+        ctx_check(w->S.ctx);
+        halo_copy(w->S, side, to_ghost ? 1 : 0, d_buf, stream ? static_cast<cudaStream_t>(stream) : w->S.ctx->stream);
+    });
+}
+
+bd_status bd_halo_exchange(bd_westervelt* lower, bd_westervelt* upper) {
+    return guard([&] {
+        if (!lower || !upper) fail(BD_ERR_INVALID_ARG, "null session");
+        if (lower->S.ctx != upper->S.ctx) fail(BD_ERR_INVALID_ARG, "same-device exchange needs one context");
+        ctx_check(lower->S.ctx);
+        halo_exchange(lower->S, upper->S, lower->S.ctx->stream);
+    });
+}
+
+bd_status bd_westervelt_run_slabs(bd_context* ctx, const bd_grid* grid, const bd_medium* medium,
+                                  const bd_source* source, const bd_westervelt_params* params, int32_t n_slabs,
+                                  bd_westervelt_outputs* out) {
+    return guard([&] {
+        if (!out || !grid || !params) fail(BD_ERR_INVALID_ARG, "null argument");
+        ctx_check(ctx);
+        if (n_slabs < 1 || n_slabs > grid->nz / 8) fail(BD_ERR_INVALID_ARG, "n_slabs must be 1..nz/8");
+        const long long plane = (long long)grid->nx * grid->ny;
+        std::vector<int> zb(n_slabs + 1);
+        for (int k = 0; k <= n_slabs; ++k) zb[k] = (int)((long long)grid->nz * k / n_slabs);
+        std::vector<std::unique_ptr<WvSession>> sl;
+        for (int k = 0; k < n_slabs; ++k) {
+            sl.emplace_back(new WvSession());
+            if (n_slabs == 1) setup(*sl[k], ctx, grid, medium, source, params);
+            else setup_slab(*sl[k], ctx, grid, medium, source, params, zb[k], zb[k + 1]);
+        }
+        cudaStream_t st = ctx->stream;
+        BD_CUDA(cudaEventRecord(ctx->ev0, st));
+        for (int64_t s = 0; s < params->n_steps; ++s) {
+            for (auto& S : sl) {
+                issue_steps(*S, S->variant, S->step, 1, st);
+                S->step += 1;
+            }
+            for (int k = 0; k + 1 < n_slabs; ++k) halo_exchange(*sl[k], *sl[k + 1], st);
+        }
+        BD_CUDA(cudaEventRecord(ctx->ev1, st));
+        BD_CUDA(cudaEventSynchronize(ctx->ev1));
+        float ms = 0;
+        BD_CUDA(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+        for (auto& S : sl) {
+            unsigned f = 0;
+            BD_CUDA(cudaMemcpy(&f, S->flag.as<unsigned>() + 1, sizeof f, cudaMemcpyDeviceToHost));
+            if (f & 4u) fail(BD_ERR_TIMEOUT, "a pipeline wait in the stencil kernel timed out");
+        }
+        // each slab writes its owned planes into the whole grid's outputs
+        for (int k = 0; k < n_slabs; ++k) {
+            WvSession& S = *sl[k];
+            bd_westervelt_outputs o = *out;
+            const size_t off = (size_t)zb[k] * plane;
+            if (out->p_final) o.p_final = static_cast<char*>(out->p_final) + off * S.esz;
+            if (out->peak) o.peak = static_cast<char*>(out->peak) + off * S.esz;
+            if (out->energy) o.energy = static_cast<char*>(out->energy) + off * S.esz;
+            if (out->Q) o.Q = out->Q + off;
+            finish(S, &o);
+        }
+        out->steps_done = params->n_steps;
+        out->tile_variant = sl[0]->variant;
+        out->elapsed_ms = ms;
     });
 }
 

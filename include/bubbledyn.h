@@ -231,6 +231,49 @@ bd_status bd_checkpoint_load(bd_westervelt* wv, const void* blob, size_t bytes);
 bd_status bd_westervelt_last_ms(bd_westervelt* wv, double* ms);
 
 /* ------------------------------------------------------------------------- */
+/* z-slab domain decomposition of the Westervelt solve                        */
+/* ------------------------------------------------------------------------- */
+/* The reference runs one grid on one device (cudaSetDevice(0), W:353); these
+ * calls split the grid into slabs of whole z planes, one per device (or
+ * several on one device).  The 6th-order stencil reads p^n at iz-3..iz+3
+ * (W:169-174), so a slab keeps 3 ghost planes beyond each internal face,
+ * copied from the neighbour after every step; everything else a step reads is
+ * cell-local.  With the ghosts refreshed after every step, the owned planes
+ * evolve bit for bit as in one session over the whole grid.
+ *
+ * bd_westervelt_slab_begin: a session for the planes [z_begin, z_end) of the
+ * whole problem (grid, medium, source, params describe the whole grid; at least
+ * 8 owned planes; Mur layers of the z faces must lie inside the end slabs).
+ * Advance it ONE step at a time and refresh the ghosts between steps.  finish()
+ * writes the owned planes only: p_final / peak / energy / Q hold
+ * nx*ny*(z_end - z_begin) values, dft_re / dft_im the owned planes inside
+ * [dft_z_lo, dft_z_hi). */
+bd_status bd_westervelt_slab_begin(bd_context* ctx, const bd_grid* grid, const bd_medium* medium,
+                                   const bd_source* source, const bd_westervelt_params* params, int32_t z_begin,
+                                   int32_t z_end, bd_westervelt** out);
+/* Bytes of one halo message: 3 planes of nx*ny cells of the field type. */
+bd_status bd_westervelt_halo_bytes(bd_westervelt* wv, size_t* bytes);
+/* Halo transfer of the newest pressure level through a device buffer of
+ * bd_westervelt_halo_bytes: to_ghost = 0 copies the 3 owned planes next to
+ * internal face `side` (0 = low z, 1 = high z) into d_buf (the message for that
+ * neighbour); to_ghost = 1 copies d_buf into the 3 ghost planes beyond it.
+ * Enqueued on stream (NULL = the context's stream); the transport between
+ * devices (NCCL send/recv, or a copy into the receiver's own memory) is the
+ * caller's. */
+bd_status bd_westervelt_halo_copy(bd_westervelt* wv, int32_t side, int32_t to_ghost, void* d_buf, void* stream);
+/* Same-device exchange between neighbouring slabs of one context (lower owns
+ * the planes just below upper's): both directions, enqueued on the context's
+ * stream. */
+bd_status bd_halo_exchange(bd_westervelt* lower, bd_westervelt* upper);
+/* The whole solve as n_slabs equal slabs on this context's device, with the
+ * ghost planes exchanged after every step; outputs as bd_westervelt_run (the
+ * whole grid).  Checks the decomposition: its results equal bd_westervelt_run's
+ * bit for bit. */
+bd_status bd_westervelt_run_slabs(bd_context* ctx, const bd_grid* grid, const bd_medium* medium,
+                                  const bd_source* source, const bd_westervelt_params* params, int32_t n_slabs,
+                                  bd_westervelt_outputs* out);
+
+/* ------------------------------------------------------------------------- */
 /* Adjoint Westervelt (phased-array gradients)                                */
 /* ------------------------------------------------------------------------- */
 

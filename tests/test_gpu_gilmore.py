@@ -135,3 +135,39 @@ def test_static_schedule_gives_the_same_bits_as_persistent(ctx):
     r2, _ = ctx.gilmore(med, b, ode)
     for k in ("R", "Rdot", "tau", "q", "t", "R_max", "R_min", "n_accept", "n_reject", "status"):
         np.testing.assert_array_equal(r1[k], r2[k])
+
+
+def test_fast_path_at_full_cfg2_drive_matches_oracle(ctx, oracle):
+    """The first 256 bubbles of the cfg2 set at their full 0.5-3 MPa three-tone
+    drive with random phases, over 2 us (most of them collapse, where the
+    step-start expansions hand over to direct transcendentals): R, R_max within
+    1e-6 of the FP64 oracle and the same threshold flag for every bubble."""
+    med = presets.cfg2_medium()
+    b = presets.cfg2_bubbles(1 << 20)[:256]
+    ode = presets.cfg2_ode(t_end=2e-6)
+    res, ms = ctx.gilmore(med, b, ode)
+    ro = oracle.gilmore(med, to_ctypes(b), ode)
+    R = np.array([r.R for r in ro])
+    Rmax = np.array([r.R_max for r in ro])
+    thr = np.array([r.threshold for r in ro])
+    assert np.all(res["status"] == abi.BD_BUBBLE_DONE)
+    assert thr.sum() > 64                       # the drive collapses a good share of them
+    assert (res["R_max"] / b["R0"]).max() > 10.0
+    np.testing.assert_allclose(res["R"], R, rtol=1e-6)
+    np.testing.assert_allclose(res["R_max"], Rmax, rtol=1e-6)
+    np.testing.assert_array_equal(res["threshold"], thr)
+
+
+def test_threshold_search_uncapped_fixture_item(ctx):
+    """One uncapped item of G's search (G:323-429) on the GPU against the
+    reference's own result: the fixture item with the lowest threshold
+    (combination 27670, R0 = 2 um, 2.408 MPa), so stage 1 climbs 25 amplitudes
+    and stages 2 and 3 (10 kPa and 1 kPa descents with h reset, G:390-426)
+    run on the device.  Fast right-hand side: one lane carries the item, and at
+    G's 1e-9 tolerances it takes about 4 minutes of this GPU (G's operation
+    order would take about six times longer)."""
+    g = np.load(golden_path("G_threshold.npz"))
+    A, ms = ctx.gilmore_threshold(presets.ref_G_medium(), g["combos"][3:4], g["R0"][0:1], ref_arith=0, max_steps=0)
+    print("uncapped threshold item: %.1f s" % (ms * 1e-3))
+    assert A[0, 0] == g["A"][3, 0]
+    assert A[0, 0] % 1e5 != 0                   # the result comes from the 1 kPa stage
