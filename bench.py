@@ -307,47 +307,46 @@ def adjoint_summary(ctx):
     return out
 
 
-HEAT_BYTES_PER_CELL = 28    # theta read + write 8 B, Q 4 B, dose (FP32 pair) read + write 16 B
+HEAT_BYTES_PER_CELL = 28    # theta read + write 8 B, Q 4 B, FP64 dose read + write 16 B
 
 
-def cfg3_summary(ctx, sample_spots=2):
-    """cfg3: the acoustic solve (25.2 M cells, CW until ten periods after the
-    front crossed the box), the W -> T hand-off, and `sample_spots` of the 49
-    spiral spots of bioheat + CEM43 dose (2000 steps of 1 ms each)."""
+def cfg3_summary(ctx, n_spots=49):
+    """cfg3 in full: the acoustic solve (25.2 M cells, CW until ten periods
+    after the front crossed the box), the W -> T hand-off, and all 49 spiral
+    spots of bioheat + CEM43 dose (2000 steps of 1 ms each, 98,000 steps)."""
     from bubbledynamics_gb300 import pipeline, presets
     pk, pk_kind = peaks()
     ac = presets.cfg3_acoustic()
     g = ac.grid
     ncell = g.nx * g.ny * g.nz
     t0 = time.perf_counter()
-    res = pipeline.cfg3_run(ctx, acoustic=ac, n_spots=sample_spots)
+    res = pipeline.cfg3_run(ctx, acoustic=ac, n_spots=n_spots)
     wall = time.perf_counter() - t0
     n = ac.params.n_steps
     heat_steps = res["heat_steps"]
     heat_us = res["heat_ms"] * 1e3 / heat_steps
     achieved = HEAT_BYTES_PER_CELL * ncell / (heat_us * 1e-6) / 1e9
-    full_steps = 49 * 2000
     return {
         "workload": "cfg3 liver heating, 256x256x384, FP32 Westervelt (%d steps) -> Q -> %d of 49 spots x 2000 "
-                    "heat steps (FP32 dT, double-float dose)" % (n, sample_spots),
+                    "heat steps (FP32 dT, FP64 dose)" % (n, n_spots),
         "acoustic_ms": res["acoustic_ms"], "acoustic_gcells": ncell * n / (res["acoustic_ms"] * 1e-3) / 1e9,
         "heat_ms": res["heat_ms"], "heat_steps": heat_steps, "heat_us_per_step": heat_us,
         "heat_gcells": ncell / (heat_us * 1e-6) / 1e9,
         "heat_roofline": {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
                           "frac": achieved / pk["hbm_gbs"], "algorithmic_bytes": HEAT_BYTES_PER_CELL * ncell,
                           "peak_kind": pk_kind},
-        "projected_full_run_s": (res["acoustic_ms"] + heat_us * full_steps * 1e-3) * 1e-3,
+        "full_run_s": (res["acoustic_ms"] + res["heat_ms"]) * 1e-3,
         "focal_peak_mpa": float(res["peak"].max() / 1e6),
         "T_max_C": float(res["T"].max() - 273.15), "dose_max_min": float(res["dose"].max() / 60.0),
         "wall_s": wall,
     }
 
 
-def cfg5_summary(ctx, n_steps=4000, n_bubbles=1 << 16, t_end=0.1e-6):
-    """cfg5 at full size (512x512x768, 2 relaxation processes, three tones, the
-    9-frequency DFT over the last 10 us on the 200 planes around the focus),
-    shortened to n_steps time steps; then n_bubbles bubbles at random
-    focal-region points driven by the DFT-reconstructed local pressure."""
+def cfg5_summary(ctx, n_steps=12000, n_bubbles=1 << 18, t_end=0.1e-6):
+    """cfg5 in full (512x512x768, 2 relaxation processes, three tones, 12,000
+    steps, the 9-frequency DFT over the last 10 us on the 200 planes around the
+    focus); then n_bubbles bubbles at random focal-region points driven by the
+    DFT-reconstructed local pressure for t_end."""
     from bubbledynamics_gb300 import pipeline, presets
     pk, pk_kind = peaks()
     prob = presets.cfg5(n_steps=n_steps)
@@ -369,9 +368,10 @@ def cfg5_summary(ctx, n_steps=4000, n_bubbles=1 << 16, t_end=0.1e-6):
     dft_cells = (p.dft_z_hi - p.dft_z_lo) * g.nx * g.ny
     win_bytes = (b_cell + 8) * ncell + 16 * p.n_dft * dft_cells
     win_us = win_ms * 1e3 / p.dft_len
-    out = {"workload": "cfg5 512x512x768 FP32, %d of 12000 steps, 9-frequency DFT over the last 10 us (530 steps) "
+    out = {"workload": "cfg5 512x512x768 FP32, %d steps, 9-frequency DFT over the last 10 us (530 steps) "
                        "on %d planes; %d bubbles driven by the local field for %g s" % (n_steps, p.dft_z_hi - p.dft_z_lo,
                                                                                          n_bubbles, t_end),
+           "run_s": (out_us * p.dft_start + win_ms * 1e3) * 1e-6,
            "us_per_step_outside_window": out_us, "gcells_outside_window": ncell / (out_us * 1e-6) / 1e9,
            "roofline_outside_window": {"achieved": b_cell * ncell / (out_us * 1e-6) / 1e9, "peak": pk["hbm_gbs"],
                                        "frac": b_cell * ncell / (out_us * 1e-6) / 1e9 / pk["hbm_gbs"],
@@ -379,24 +379,30 @@ def cfg5_summary(ctx, n_steps=4000, n_bubbles=1 << 16, t_end=0.1e-6):
            "us_per_step_in_window": win_us,
            "roofline_in_window": {"achieved": win_bytes / (win_us * 1e-6) / 1e9, "peak": pk["hbm_gbs"],
                                   "frac": win_bytes / (win_us * 1e-6) / 1e9 / pk["hbm_gbs"], "unit": "GB/s"},
-           "projected_12000_steps_s": (out_us * (12000 - p.dft_len) + win_us * p.dft_len) * 1e-6,
            "focal_peak_mpa": float(r["peak"].max() / 1e6)}
     b, _ = pipeline.bubbles_from_dft(prob, r["dft_re"], r["dft_im"], n_bubbles)
     res, ms = ctx.gilmore(presets.cfg2_medium(), b, presets.cfg2_ode(t_end=t_end))
     att = float(res["n_accept"].sum() + res["n_reject"].sum())
-    out["bubbles"] = {"ms": ms, "attempts_per_s": att / (ms * 1e-3), "threshold_fraction": float(res["threshold"].mean()),
+    out["bubbles"] = {"n": n_bubbles, "t_end_s": t_end, "ms": ms, "attempts_per_s": att / (ms * 1e-3),
+                      "threshold_fraction": float(res["threshold"].mean()),
                       "R_max_over_R0_median": float(np.median(res["R_max"] / b["R0"]))}
+    out["run_with_bubbles_s"] = out["run_s"] + ms * 1e-3
     return out
 
 
-def gilmore_summary(ctx, n=1 << 17, t_end=0.5e-6, cpu_n=1024, with_cpu=True):
-    """cfg2 bubbles (first n of the 2^20 set) over a bounded window; the CPU
-    oracle on the first cpu_n of them over the same window, all host cores."""
+def gilmore_summary(ctx, n=1 << 20, t_end=0.004e-6, cpu_n=1 << 14, with_cpu=True):
+    """cfg2 bubbles (all 2^20 by default) over a bounded window through three
+    kernels: the persistent work-stealing fast path, the same arithmetic one
+    thread per bubble (static), and the naive baseline: one thread per bubble
+    in the reference's operation order (7 right-hand sides with their pow calls
+    per attempt, G:212-318) at the same cfg2 settings (phases, rtol 1e-8).  The
+    CPU oracle runs the first cpu_n of them over the same window, all host
+    cores."""
     import numpy as np
     from bubbledynamics_gb300 import abi, presets
     med = presets.cfg2_medium()
     b = presets.cfg2_bubbles(1 << 20)[:n]
-    out = {"workload": "cfg2 Gilmore FP64, first %d of the 2^20 seeded bubbles, t = 0..%g s, rtol 1e-8" % (n, t_end)}
+    out = {"workload": "cfg2 Gilmore FP64, %d of the 2^20 seeded bubbles, t = 0..%g s, rtol 1e-8" % (n, t_end)}
     if with_cpu:
         from oracle.oracle import Oracle
         orc = Oracle()
@@ -407,16 +413,20 @@ def gilmore_summary(ctx, n=1 << 17, t_end=0.5e-6, cpu_n=1024, with_cpu=True):
         out["cpu_baseline"] = {"bubbles_per_s": cpu_n / dt, "bubble_us_per_s": cpu_n * t_end * 1e6 / dt,
                                "cores": orc.threads(), "kind": "port",
                                "sample": "first %d bubbles, same window, FP64 oracle (OpenMP)" % cpu_n}
-    for name, sched in (("persistent", abi.BD_SCHEDULE_PERSISTENT), ("static", abi.BD_SCHEDULE_STATIC)):
+    for name, sched, ref in (("persistent", abi.BD_SCHEDULE_PERSISTENT, 0), ("static", abi.BD_SCHEDULE_STATIC, 0),
+                             ("naive_static", abi.BD_SCHEDULE_STATIC, 1)):
         o = presets.cfg2_ode(t_end=t_end)
         o.schedule = sched
+        o.ref_arith = ref
         r, ms = ctx.gilmore(med, b, o)
         att = float(r["n_accept"].sum() + r["n_reject"].sum())
         out[name] = {"ms": ms, "bubbles_per_s": n / (ms * 1e-3), "attempts_per_s": att / (ms * 1e-3),
                      "bubble_us_per_s": n * t_end * 1e6 / (ms * 1e-3)}
-    acc = r["n_accept"].astype(np.float64)
+        if name == "persistent":
+            acc = r["n_accept"].astype(np.float64)
     out["accepted_steps"] = {"mean": float(acc.mean()), "max": float(acc.max())}
     out["speedup_vs_static"] = out["static"]["ms"] / out["persistent"]["ms"]
+    out["speedup_vs_naive_static"] = out["naive_static"]["ms"] / out["persistent"]["ms"]
     return out
 
 
@@ -481,10 +491,11 @@ def run_gilmore(args):
     b = presets.cfg2_bubbles(1 << 20)[:args.bubbles]
     o = presets.cfg2_ode(t_end=args.t_end)
     o.schedule = abi.BD_SCHEDULE_STATIC if args.schedule == "static" else abi.BD_SCHEDULE_PERSISTENT
+    o.ref_arith = 1 if args.ref_arith else 0
     r, ms = ctx.gilmore(med, b, o)
     att = float(r["n_accept"].sum() + r["n_reject"].sum())
     print(json.dumps({"workload": "cfg2 Gilmore sample", "bubbles": args.bubbles, "t_end": args.t_end,
-                      "schedule": args.schedule, "ms": ms, "attempts": int(att),
+                      "schedule": args.schedule, "ref_arith": int(o.ref_arith), "ms": ms, "attempts": int(att),
                       "attempts_per_s": att / (ms * 1e-3)}), flush=True)
     ctx.close()
 
@@ -562,6 +573,7 @@ def main():
     ap.add_argument("--bubbles", type=int, default=1 << 16, help="gilmore workload: bubbles")
     ap.add_argument("--t-end", type=float, default=2e-6, help="gilmore workload: window [s]")
     ap.add_argument("--schedule", default="persistent", choices=["persistent", "static"])
+    ap.add_argument("--ref-arith", action="store_true", help="gilmore workload: the reference's operation order")
     ap.add_argument("--time-steps", type=int, default=30, help="step-kernel workload: time steps per solve")
     ap.add_argument("--tile-variant", type=int, default=-1,
                     help="step-kernel / dft workloads: tile variant (-1: every TMA variant / autotuned)")

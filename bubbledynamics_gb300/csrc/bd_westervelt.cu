@@ -1162,9 +1162,45 @@ static void adjoint_solve(WvSession& S, const bd_focal_loss* loss, double* loss_
             segQ[j] = make_map(S, seg[j].p, fl, var.tx, var.ty);
         }
     }
-    auto store_segment = [&](int64_t s0, int64_t s1) {
-        for (int k = 0; k < 5; ++k)
-            BD_CUDA(cudaMemcpyAsync(seg[4 - k].p, S.P[(head_of(s0) + k) % 5].p, f, cudaMemcpyDeviceToDevice, st));
+    // Whole segments of Kc steps (the recompute and the backward sweep) replay
+    // captured CUDA graphs: a step's buffers depend only on its place in the
+    // segment, the parity of its index (relaxation ring) and the number of
+    // backward steps done modulo 6 (adjoint rings), and its index comes from a
+    // device counter, so one graph per key serves every full segment.
+    const bool use_graphs = S.p.graph_chunk >= 0;
+    struct GraphCache {
+        std::map<int, cudaGraphExec_t> g;
+        ~GraphCache() { for (auto& kv : g) cudaGraphExecDestroy(kv.second); }
+    } rec_graphs, bwd_graphs;
+    auto captured = [&](GraphCache& cache, int key, int64_t launches, auto&& body) {
+        auto it = cache.g.find(key);
+        if (it == cache.g.end()) {
+            cudaStream_t cs;
+            BD_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+            cudaGraph_t gr = nullptr;
+            const int64_t before = S.ctx->launches;
+            BD_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+            try {
+                body(cs);
+            } catch (...) {
+                cudaStreamEndCapture(cs, &gr);
+                if (gr) cudaGraphDestroy(gr);
+                cudaStreamDestroy(cs);
+                throw;
+            }
+            BD_CUDA(cudaStreamEndCapture(cs, &gr));
+            S.ctx->launches = before;      // captured, not launched
+            cudaGraphExec_t ex = nullptr;
+            const cudaError_t e = cudaGraphInstantiate(&ex, gr, 0);
+            cudaGraphDestroy(gr);
+            cudaStreamDestroy(cs);
+            BD_CUDA(e);
+            it = cache.g.emplace(key, ex).first;
+        }
+        BD_CUDA(cudaGraphLaunch(it->second, st));
+        S.ctx->launches += launches;
+    };
+    auto segment_steps = [&](cudaStream_t cs, int64_t s0, int64_t s1) {
         for (int64_t s = s0; s < s1; ++s) {
             const int64_t j = s - s0;            // seg[j .. j+4] = p^{s-4} .. p^s
             if (seg_direct) {
@@ -1172,14 +1208,28 @@ static void adjoint_solve(WvSession& S, const bd_focal_loss* loss, double* loss_
                 S.segv.p0 = segP0[j + 4];
                 for (int k = 0; k < 4; ++k) S.segv.q[k] = segQ[j + 3 - k];
                 S.segv.out = seg[j + 5].p;
-                issue_steps(S, S.variant, s, 1, st);
+                try {
+                    issue_steps(S, S.variant, s, 1, cs);
+                } catch (...) {
+                    S.segv.on = false;
+                    throw;
+                }
                 S.segv.on = false;
             } else {
-                issue_steps(S, S.variant, s, 1, st);
-                BD_CUDA(cudaMemcpyAsync(seg[j + 5].p, S.P[head_of(s + 1)].p, f, cudaMemcpyDeviceToDevice, st));
+                issue_steps(S, S.variant, s, 1, cs);
+                BD_CUDA(cudaMemcpyAsync(seg[j + 5].p, S.P[head_of(s + 1)].p, f, cudaMemcpyDeviceToDevice, cs));
             }
-            S.step = s + 1;
         }
+    };
+    auto store_segment = [&](int64_t s0, int64_t s1) {
+        for (int k = 0; k < 5; ++k)
+            BD_CUDA(cudaMemcpyAsync(seg[4 - k].p, S.P[(head_of(s0) + k) % 5].p, f, cudaMemcpyDeviceToDevice, st));
+        if (use_graphs && seg_direct && s1 - s0 == Kc)
+            captured(rec_graphs, (int)(s0 & 1), Kc * (launches_per_step(S) + 1),
+                     [&](cudaStream_t cs) { segment_steps(cs, s0, s1); });
+        else
+            segment_steps(st, s0, s1);
+        S.step = s1;
     };
     auto level_buf = [&](int64_t s, int k) -> PoolBuf& {   // k < 5: p^{s-k}; 5 + 2v + j: R^{s-1-j} of process v
         if (k < 5) return S.P[(head_of(s) + k) % 5];
@@ -1287,7 +1337,39 @@ static void adjoint_solve(WvSession& S, const bd_focal_loss* loss, double* loss_
     a.burst_lenf = (float)a.burst_len;
     a.fx = loss->focus_ix; a.fy = loss->focus_iy; a.fz = loss->focus_iz;
     a.frad2 = fr2; a.srad2 = sr2; a.side_w = loss->side_weight;
-    int rot = 0, rrot = 0;    // rotation of the adjoint rings
+    // backward step counter on the device: forward index of the next backward step
+    PoolBuf bstep;
+    bstep.alloc(S.ctx, 64);
+    {
+        const long long last = N - 1;
+        BD_CUDA(cudaMemcpyAsync(bstep.p, &last, sizeof last, cudaMemcpyHostToDevice, st));
+        BD_CUDA(cudaStreamSynchronize(st));
+    }
+    a.bstep = bstep.as<long long>();
+    a.win0 = loss->window_start;
+    a.win1 = loss->window_end;
+    // backward steps s1-1 .. s0 of a segment after nb earlier backward steps
+    auto backward_steps = [&](cudaStream_t cs, int64_t s0, int64_t s1, int64_t nb) {
+        int rot = (int)(nb % 6), rrot = (int)(nb % 3);    // rotation of the adjoint rings
+        int koff = 0;
+        for (int64_t s = s1 - 1; s >= s0; --s, ++koff) {
+            for (int k = 0; k < 5; ++k) a.mu[k] = mu[(rot + k) % 6].as<real>();
+            a.mu5 = mu[(rot + 5) % 6].as<real>();
+            for (int v = 0; v < S.max_relax; ++v) {
+                a.muR1[v] = muR[v][rrot].as<real>();
+                a.muR2[v] = muR[v][(rrot + 1) % 3].as<real>();
+                a.muR3[v] = muR[v][(rrot + 2) % 3].as<real>();
+            }
+            for (int k = 0; k < 5; ++k) a.fp[k] = seg[s - s0 + 5 - k].as<real>();
+            a.koff = koff;
+            adj_launch<real>(S, a, cs);
+            rot = (rot + 1) % 6;      // lambda_k now sits in the buffer of mu_{k+1}, lambda_4 in the spare
+            rrot = (rrot + 1) % 3;
+        }
+        adj_advance_kernel<<<1, 32, 0, cs>>>(bstep.as<long long>(), (int)(s1 - s0));
+        BD_LAUNCHED(S.ctx);
+    };
+    int64_t nb_done = 0;
     float ms_rec = 0, ms_bwd = 0;
     for (int64_t c = nck - 1; c >= 0; --c) {
         const int64_t s0 = c * Kc, s1 = std::min<int64_t>(N, s0 + Kc);
@@ -1302,21 +1384,13 @@ static void adjoint_solve(WvSession& S, const bd_focal_loss* loss, double* loss_
             store_segment(s0, s1);
         }
         BD_CUDA(cudaEventRecord(S.ctx->ev1, st));
-        for (int64_t s = s1 - 1; s >= s0; --s) {
-            for (int k = 0; k < 5; ++k) a.mu[k] = mu[(rot + k) % 6].as<real>();
-            a.mu5 = mu[(rot + 5) % 6].as<real>();
-            for (int v = 0; v < S.max_relax; ++v) {
-                a.muR1[v] = muR[v][rrot].as<real>();
-                a.muR2[v] = muR[v][(rrot + 1) % 3].as<real>();
-                a.muR3[v] = muR[v][(rrot + 2) % 3].as<real>();
-            }
-            for (int k = 0; k < 5; ++k) a.fp[k] = seg[s - s0 + 5 - k].as<real>();
-            a.step = s;
-            a.in_window = (s >= loss->window_start && s < loss->window_end) ? 1 : 0;
-            adj_launch<real>(S, a, st);
-            rot = (rot + 1) % 6;      // lambda_k now sits in the buffer of mu_{k+1}, lambda_4 in the spare
-            rrot = (rrot + 1) % 3;
+        if (use_graphs && s1 - s0 == Kc) {
+            const int64_t nb = nb_done;
+            captured(bwd_graphs, (int)(nb % 6), 2 * Kc + 1, [&](cudaStream_t cs) { backward_steps(cs, s0, s1, nb); });
+        } else {
+            backward_steps(st, s0, s1, nb_done);
         }
+        nb_done += s1 - s0;
         cudaEvent_t e2;
         BD_CUDA(cudaEventCreate(&e2));
         BD_CUDA(cudaEventRecord(e2, st));

@@ -69,9 +69,22 @@ struct AdjArgs {
     // loss
     int fx, fy, fz, frad2, srad2;
     double side_w;
-    int in_window;              // step s contributes p^{s+1} to the loss
-    long long step;             // forward step index s
+    long long win0, win1;       // loss window: step s contributes p^{s+1} when win0 <= s < win1
+    // forward step index s of this backward step = *bstep - koff: a device counter
+    // that a small kernel moves after each chunk of backward steps, so one captured
+    // CUDA graph of a chunk serves every segment of the sweep
+    const long long* bstep;
+    int koff;
 };
+
+template <class real>
+__device__ __forceinline__ long long adj_step(const AdjArgs<real>& a) {
+    return *a.bstep - a.koff;
+}
+
+__global__ void adj_advance_kernel(long long* bstep, int n) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) *bstep -= n;
+}
 
 template <class real>
 __device__ __forceinline__ int adj_mat(const AdjArgs<real>& a, long long i, int iz) {
@@ -95,11 +108,11 @@ __device__ __forceinline__ real loss_weight(const AdjArgs<real>& a, int ix, int 
 }
 
 // d S_j / d phi_e and S_j (FP64 path, W:78-82 plus tones, bursts, elements)
-__device__ __forceinline__ void src_derivs(const AdjArgs<double>& a, int j, double& S, double& dphi) {
+__device__ __forceinline__ void src_derivs(const AdjArgs<double>& a, long long step, int j, double& S, double& dphi) {
     S = 0.0; dphi = 0.0;
     const double A = a.sA[j];
     if (A == 0.0) return;
-    double tt = a.t_src[a.step] + a.sTau[j];
+    double tt = a.t_src[step] + a.sTau[j];
     if (a.burst) {
         const double tb = tt - a.tau_max;
         if (tb < 0.0 || tb >= a.burst_len) return;
@@ -115,18 +128,18 @@ __device__ __forceinline__ void src_derivs(const AdjArgs<double>& a, int j, doub
     dphi = A * c / a.sVar[j];
 }
 
-__device__ __forceinline__ void src_derivs(const AdjArgs<float>& a, int j, float& S, float& dphi) {
+__device__ __forceinline__ void src_derivs(const AdjArgs<float>& a, long long step, int j, float& S, float& dphi) {
     S = 0.0f; dphi = 0.0f;
     const float A = a.sAf[j];
     if (A == 0.0f) return;
     if (a.burst) {
-        const float tb = a.tb0[a.step] + a.sTauf[j];
+        const float tb = a.tb0[step] + a.sTauf[j];
         if (tb < 0.0f || tb >= a.burst_lenf) return;
     }
     float s = 0.0f, c = 0.0f;
     for (int k = 0; k < a.n_tones; ++k) {
         float sn, cs;
-        sincosf(add_(a.theta[a.step * BD_MAX_TONES + k], a.sPsi[(long long)k * a.plane + j]), &sn, &cs);
+        sincosf(add_(a.theta[step * BD_MAX_TONES + k], a.sPsi[(long long)k * a.plane + j]), &sn, &cs);
         s = fma_(a.tampf[k], sn, s);
         c = fma_(a.tampf[k], cs, c);
     }
@@ -243,13 +256,14 @@ __global__ void __launch_bounds__(256) adj_point_kernel(const AdjArgs<real> a, c
     const int iz = (int)(i0 / a.plane);
     const long long col0 = i0 - (long long)iz * a.plane;
     const int iy = (int)(col0 / a.nx), ix0 = (int)(col0 - (long long)iy * a.nx);
+    const long long step = adj_step(a);
     Vec<real, VEC> m0 = vload<real, VEC>(a.mu[0] + i0);
     Vec<real, VEC> l0 = vload<real, VEC>(a.mu[1] + i0);
     Vec<real, VEC> l1 = vload<real, VEC>(a.mu[2] + i0);
     Vec<real, VEC> l2 = vload<real, VEC>(a.mu[3] + i0);
     Vec<real, VEC> l3 = vload<real, VEC>(a.mu[4] + i0);
     Vec<real, VEC> l4, h;
-    if (a.in_window) {
+    if (step >= a.win0 && step < a.win1) {
         const bool hit = abs(iz - a.fz) * abs(iz - a.fz) <= max(a.frad2, 0) || iz == a.fz;
         if (hit) {
 #pragma unroll
@@ -264,7 +278,7 @@ __global__ void __launch_bounds__(256) adj_point_kernel(const AdjArgs<real> a, c
         for (int k = 0; k < VEC; ++k) {
             const int col = (int)col0 + k;
             real S, dphi;
-            src_derivs(a, col, S, dphi);
+            src_derivs(a, step, col, S, dphi);
             a.gphi[col] += (double)m0.v[k] * (double)dphi;
             const double ea = a.e_amp[col];
             if (ea != 0.0) a.gamp[col] += (double)m0.v[k] * (double)S / ea;

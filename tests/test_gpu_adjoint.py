@@ -73,6 +73,23 @@ def test_adjoint_gradient_independent_of_checkpoint_interval(ctx, prec):
             np.testing.assert_array_equal(ga, ref[2])
 
 
+@pytest.mark.parametrize("prec", [abi.BD_F64, abi.BD_F32])
+def test_adjoint_graphs_and_plain_launches_identical(ctx, prec):
+    """The recompute and backward sweeps replayed as captured CUDA graphs (one
+    per segment parity and adjoint-ring rotation) give the bits of plain
+    launches, for segment lengths that are odd, even and longer than 6."""
+    for k in (7, 8, 15, 0):
+        res = []
+        for chunk in (0, -1):
+            prob, loss = presets.adjoint_mini(precision=prec)
+            prob.params.graph_chunk = chunk
+            loss.checkpoint_every = k
+            res.append(ctx.westervelt_adjoint(prob, loss))
+        assert res[0][0] == res[1][0], k
+        np.testing.assert_array_equal(res[0][1], res[1][1], err_msg="phase, K = %d" % k)
+        np.testing.assert_array_equal(res[0][2], res[1][2], err_msg="amplitude, K = %d" % k)
+
+
 def test_adjoint_f32_close_to_f64_oracle(ctx, oracle):
     p64, loss = presets.adjoint_mini(precision=abi.BD_F64)
     _, gpo, gao = oracle.westervelt_adjoint(p64, loss)
