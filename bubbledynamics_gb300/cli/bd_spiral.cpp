@@ -143,9 +143,9 @@ int main(int argc, char** argv) {
     // slice positions of T:424-445 and T:578-636 from their coordinates, clipped to the box
     const int h = k.Nxy_half;
     const int x0 = clampi(h - 100, 0, Nxy), x1 = clampi(h + 101, 0, Nxy), x1d = clampi(h + 102, 0, Nxy);
-    const int z12 = clampi((int)std::lround(0.12 / k.dz), 0, Nz - 1);
-    int zr0 = z12, zr1 = clampi((int)std::lround(0.17 / k.dz) + 1, 0, Nz), zd1 = clampi((int)std::lround(0.16 / k.dz) + 1, 0, Nz);
-    if (zr1 <= zr0 || zd1 <= zr0) { zr0 = 0; zr1 = Nz; zd1 = Nz; }   // a box shorter than 12 cm: every plane
+    int zr0 = (int)std::lround(0.12 / k.dz);
+    int zr1 = clampi((int)std::lround(0.17 / k.dz) + 1, 0, Nz), zd1 = clampi((int)std::lround(0.16 / k.dz) + 1, 0, Nz);
+    if (zr0 >= Nz) { zr0 = 0; zr1 = Nz; zd1 = Nz; }   // a box shorter than 12 cm: every plane
     auto plane_at = [&](double z) { return clampi((int)std::lround(z / k.dz), 0, Nz - 1); };
     char name[256];
     for (size_t s = 0; s < legs.size(); ++s) {

@@ -80,8 +80,8 @@ struct WvSession {
     PoolBuf step_base, flag, kconst, Qd;
     double tau_max = 0.0;
     double last_ms = 0.0;
-    cudaGraphExec_t graph = nullptr;
-    int graph_variant = -1;
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};   // chunk graphs: [1] for chunks that accumulate nothing
+    int graph_variant[2] = {-1, -1};
     // tensor maps of the TMA variant in use (built per tile shape)
     int maps_tx = 0, maps_ty = 0;
     // adjoint: TMA map of the H buffer for the stencil pass (valid while adj_tma)
@@ -110,7 +110,8 @@ struct WvSession {
     long long dft_glob_cells = 0, dft_glob_off = 0;
 
     ~WvSession() {
-        if (graph) cudaGraphExecDestroy(graph);
+        for (auto g : graph)
+            if (g) cudaGraphExecDestroy(g);
     }
 };
 
@@ -160,13 +161,8 @@ static WvArgs<real> make_args(WvSession& S, int64_t s) {
     if (g.face[5] == kFaceHalo) a.zhi = std::min(a.zhi, S.nz - 1 - kHalo);
     if (g.sponge_cells > 0) { a.wx = S.wx.as<real>(); a.wy = S.wy.as<real>(); a.wz = S.wz.as<real>(); }
     a.dt = (real)g.dt;
-    {
-        const double kxy = g.dt * g.dt / (g.dx * g.dx) / 180.0, kz = g.dt * g.dt / (g.dz * g.dz) / 180.0;
-        a.kxy180 = (real)kxy;
-        a.kz180 = (real)kz;
-        a.kxy180l = (real)(kxy - (double)a.kxy180);
-        a.kz180l = (real)(kz - (double)a.kz180);
-    }
+    a.kxy180 = (real)(g.dt * g.dt / (g.dx * g.dx) / 180.0);
+    a.kz180 = (real)(g.dt * g.dt / (g.dz * g.dz) / 180.0);
     a.dt2 = (real)(g.dt * g.dt);
     a.dtdx = (real)(g.dt / g.dx);
     a.dtdz = (real)(g.dt / g.dz);
@@ -331,9 +327,22 @@ static void launch_tma_t(WvSession& S, const WvArgs<real>& a, int64_t s, int kof
     else launch_tma_k<real, TX, TY, CPT, -1, ZU>(S, a, maps, koff, st);
 }
 
+// Whether step s adds to any accumulator (peak, energy or DFT window open).
+static bool step_accumulates(const WvSession& S, int64_t s) {
+    return (s >= S.p.peak_start && s < S.p.peak_end) || (s >= S.p.energy_start && s < S.p.energy_end) ||
+           (S.n_dft > 0 && s >= S.p.dft_start && s < S.p.dft_start + S.p.dft_len);
+}
+
+static bool range_accumulates(const WvSession& S, int64_t s0, int64_t n) {
+    for (int64_t s = s0; s < s0 + n; ++s)
+        if (step_accumulates(S, s)) return true;
+    return false;
+}
+
 // Two x cells per thread (FP32; variant_ok has been checked).
 template <class real>
-static void launch_pair(WvSession& S, const WvArgs<real>& a, int64_t s, int koff, cudaStream_t st, const Variant& v) {
+static void launch_pair(WvSession& S, const WvArgs<real>& a, int64_t s, int koff, cudaStream_t st, const Variant& v,
+                        bool noacc) {
     if constexpr (sizeof(real) != 4) {
         fail(BD_ERR_INVALID_ARG, "two-cell tile variants take FP32 fields");
     } else {
@@ -355,6 +364,7 @@ static void launch_pair(WvSession& S, const WvArgs<real>& a, int64_t s, int koff
         c.kind = S.max_relax == 0 ? 0
                  : S.max_relax == 1 ? ((S.has_cmap && !S.has_matmap && !S.has_planemat) ? 1 : 2)
                  : S.max_relax == 2 ? 3 : -1;
+        c.noacc = noacc;
         wv_pair_launch(c);
     }
 }
@@ -368,14 +378,14 @@ static void launch_step_t(WvSession& S, const WvArgs<real>& a, int koff, cudaStr
 }
 
 template <class real>
-static void launch_step(WvSession& S, int variant, int64_t s, int koff, cudaStream_t st) {
+static void launch_step(WvSession& S, int variant, int64_t s, int koff, cudaStream_t st, bool noacc) {
     WvArgs<real> a = make_args<real>(S, s);
     const Variant& v = kVariants[variant];
     a.zb = v.zb > 0 ? v.zb : (v.zb < 0 && v.tma ? -1 : S.nz);
     if (v.tma && !tma_eligible(S)) fail(BD_ERR_INVALID_ARG, "tile variant %d needs a 16-byte row pitch", variant);
     if (!variant_ok(S, variant))
         fail(BD_ERR_INVALID_ARG, "tile variant %d takes FP32 fields with at most two relaxation processes", variant);
-    if (v.pair) launch_pair<real>(S, a, s, koff, st, v);
+    if (v.pair) launch_pair<real>(S, a, s, koff, st, v, noacc);
     else switch (variant) {
         case 0: case 3: case 7: launch_step_t<real, 32, 8>(S, a, koff, st); break;
         case 1: launch_step_t<real, 32, 4>(S, a, koff, st); break;
@@ -413,25 +423,29 @@ static void launch_step(WvSession& S, int variant, int64_t s, int koff, cudaStre
 }
 
 // Issue steps [s, s+n) on the stream (no graph): kernels read *step_base + koff,
-// then one advance kernel moves the counter by n.
-static void issue_steps(WvSession& S, int variant, int64_t s, int n, cudaStream_t st) {
+// then one advance kernel moves the counter by n.  noacc < 0: each step takes
+// the accumulator-free kernel when it accumulates nothing; 0 / 1 force it
+// off / on for every step (a captured chunk).
+static void issue_steps(WvSession& S, int variant, int64_t s, int n, cudaStream_t st, int noacc = -1) {
     for (int k = 0; k < n; ++k) {
-        if (S.prec == BD_F32) launch_step<float>(S, variant, s + k, k, st);
-        else launch_step<double>(S, variant, s + k, k, st);
+        const bool na = noacc >= 0 ? noacc != 0 : !step_accumulates(S, s + k);
+        if (S.prec == BD_F32) launch_step<float>(S, variant, s + k, k, st, na);
+        else launch_step<double>(S, variant, s + k, k, st, na);
     }
     wv_advance_kernel<<<1, 32, 0, st>>>(S.step_base.as<long long>(), n);
     BD_LAUNCHED(S.ctx);
 }
 
-static void build_graph(WvSession& S) {
-    if (S.graph) { cudaGraphExecDestroy(S.graph); S.graph = nullptr; }
+static void build_graph(WvSession& S, int noacc) {
+    cudaGraphExec_t& G = S.graph[noacc];
+    if (G) { cudaGraphExecDestroy(G); G = nullptr; }
     cudaStream_t cs;
     BD_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
     cudaGraph_t g = nullptr;
     const int64_t launches_before = S.ctx->launches;
     BD_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
     try {
-        issue_steps(S, S.variant, 0, S.chunk, cs);   // base arrangement: chunk starts at s = 0 mod 10
+        issue_steps(S, S.variant, 0, S.chunk, cs, noacc);   // base arrangement: chunk starts at s = 0 mod 10
     } catch (...) {
         cudaStreamEndCapture(cs, &g);
         if (g) cudaGraphDestroy(g);
@@ -440,10 +454,11 @@ static void build_graph(WvSession& S) {
     }
     BD_CUDA(cudaStreamEndCapture(cs, &g));
     S.ctx->launches = launches_before;   // captured, not yet launched
-    BD_CUDA(cudaGraphInstantiate(&S.graph, g, 0));
+    const cudaError_t e = cudaGraphInstantiate(&G, g, 0);
     cudaGraphDestroy(g);
     cudaStreamDestroy(cs);
-    S.graph_variant = S.variant;
+    BD_CUDA(e);
+    S.graph_variant[noacc] = S.variant;
 }
 
 static int64_t launches_per_step(const WvSession& S) {
@@ -486,8 +501,9 @@ static void advance(WvSession& S, int64_t n, bool use_graph) {
         const int64_t to_align = (S.chunk - (S.step % S.chunk)) % S.chunk;
         int64_t take;
         if (use_graph && to_align == 0 && todo >= S.chunk) {
-            if (!S.graph || S.graph_variant != S.variant) build_graph(S);
-            BD_CUDA(cudaGraphLaunch(S.graph, st));
+            const int na = range_accumulates(S, S.step, S.chunk) ? 0 : 1;
+            if (!S.graph[na] || S.graph_variant[na] != S.variant) build_graph(S, na);
+            BD_CUDA(cudaGraphLaunch(S.graph[na], st));
             S.ctx->launches += per * S.chunk + 1;
             take = S.chunk;
         } else {

@@ -39,7 +39,11 @@ __device__ __forceinline__ void st2(real* p, real v0, real v1) {
 // for more CTAs per SM.  The CTA has TX/2 x TY threads; the launch bound asks
 // for 24 resident warps per SM (at most 85 registers a thread).  The cell update is
 // cell_update(), so the results are the plain kernel's bits.
-template <class real, int TX, int TY, int NREL, int ZU, int FL, int NQ>
+//
+// NOACC: a step without any accumulation (outside the peak, energy and DFT
+// windows, e.g. the recompute of the adjoint) neither loads the peak / energy
+// tiles nor touches the accumulators: 8 B less per cell.
+template <class real, int TX, int TY, int NREL, int ZU, int FL, int NQ, bool NOACC = false>
 __global__ void __launch_bounds__(TX* TY / 2, 1536 / (TX * TY)) wv_tma_pair_kernel(const WvArgs<real> a,
                                                                  const WvConst<real>* __restrict__ Kp, int koff,
                                                                  const __grid_constant__ TmaMaps maps,
@@ -92,14 +96,16 @@ __global__ void __launch_bounds__(TX* TY / 2, 1536 / (TX * TY)) wv_tma_pair_kern
         const int plane = z0 + r;
         uint64_t* bar = &barQ[r % NQ];
         unsigned char* q = qslot(r);
-        mbar_expect_tx(bar, (unsigned)((6 + 2 * nrel) * L::QTB + (has_c ? L::QTF : 0)));
+        mbar_expect_tx(bar, (unsigned)(((NOACC ? 4 : 6) + 2 * nrel) * L::QTB + (has_c ? L::QTF : 0)));
         for (int k = 0; k < 4; ++k) tma_load_3d(q + k * L::QTB, &maps.q[k], bar, x0, y0, plane);
         for (int v = 0; v < nrel; ++v) {
             tma_load_3d(q + (4 + v) * L::QTB, &maps.rc[v], bar, x0, y0, plane);
             tma_load_3d(q + (4 + NRMAX + v) * L::QTB, &maps.ro[v], bar, x0, y0, plane);
         }
-        tma_load_3d(q + L::K_PEAK * L::QTB, &maps.peak, bar, x0, y0, plane);
-        tma_load_3d(q + L::K_ENERGY * L::QTB, &maps.energy, bar, x0, y0, plane);
+        if constexpr (!NOACC) {
+            tma_load_3d(q + L::K_PEAK * L::QTB, &maps.peak, bar, x0, y0, plane);
+            tma_load_3d(q + L::K_ENERGY * L::QTB, &maps.energy, bar, x0, y0, plane);
+        }
         if (has_c) tma_load_3d(q + L::NQR * L::QTB, &maps.cmap, bar, x0, y0, plane);
     };
 
@@ -163,10 +169,10 @@ __global__ void __launch_bounds__(TX* TY / 2, 1536 / (TX * TY)) wv_tma_pair_kern
         for (int q = TMA_NP; q < TMA_NP + 3; ++q) issueP(q);
 
     const bool fix_x = a.mir_x && x0 == 0, fix_y = a.mir_y && y0 == 0;
-    const bool do_peak = step >= a.peak_start && step < a.peak_end;
-    const bool do_energy = step >= a.energy_start && step < a.energy_end;
+    const bool do_peak = !NOACC && step >= a.peak_start && step < a.peak_end;
+    const bool do_energy = !NOACC && step >= a.energy_start && step < a.energy_end;
     const long long ds = step - a.dft_start;
-    const bool do_dft = a.n_dft > 0 && ds >= 0 && ds < a.dft_len;
+    const bool do_dft = !NOACC && a.n_dft > 0 && ds >= 0 && ds < a.dft_len;
     const bool single_mat = FL >= 0 ? (FL & 1) != 0 : (!a.matmap && !a.plane_mat);
     const bool dpdt = a.energy_mode == BD_ENERGY_DPDT2;
     // the material of single-material problems, in registers

@@ -49,14 +49,17 @@ def test_ref_mini_f64_matches_reference_fixture(ctx):
 
 
 def test_ref_mini_f32_close_to_oracle(ctx, ref_mini_oracle):
+    """FP32 on the reference physics (two layers, two relaxation processes,
+    Mur faces, the harmonic DFT): the final field and Q within the 1e-5 field
+    tolerance of the FP32 design (measured 2.0e-6 and 7.2e-7)."""
     prob, exp = ref_mini_oracle
     p32 = presets.ref_W_mini(abi.BD_F32)
     got = ctx.westervelt(p32)
     e_p = rel_l2(got["p_final"], exp["p_final"])
     e_q = rel_l2(got["Q"], exp["Q"])
     print("ref_mini f32: p_final %.3g  Q %.3g" % (e_p, e_q))
-    assert e_p < 1e-4
-    assert e_q < 1e-4
+    assert e_p < 1e-5
+    assert e_q < 1e-5
 
 
 @pytest.fixture(scope="module")
@@ -67,14 +70,15 @@ def cfg1_small_oracle(oracle):
 
 def test_cfg1_small_f32_field_accuracy(ctx, cfg1_small_oracle):
     """FP32 kernel vs FP64 oracle on the benchmark physics (heterogeneous c,
-    relaxation, sponge, burst): output maps within 1e-5 relative L2."""
+    relaxation, sponge, burst): output maps and final field within 1e-5
+    relative L2."""
     prob64, exp = cfg1_small_oracle
     prob = presets.cfg1(48, 48, 96, 600, precision=abi.BD_F32)
     got = ctx.westervelt(prob)
     e = {k: rel_l2(got[k], exp[k]) for k in ("peak", "energy", "p_final")}
     print("cfg1 small f32 errors:", e)
-    assert e["peak"] < 1e-5
-    assert e["energy"] < 1e-5
+    for k, v in e.items():
+        assert v < 1e-5, (k, v)
 
 
 def test_cfg1_small_f64_matches_oracle(ctx, cfg1_small_oracle):
@@ -319,3 +323,22 @@ def test_cfg1_full_size_f32_accuracy(ctx, cfg1_full_oracle):
     print("cfg1 full-size f32 errors:", e, "variant", got["tile_variant"])
     for k, v in e.items():
         assert v < 1e-5, (k, v)
+
+
+@pytest.mark.parametrize("chunk", [20, -1])
+def test_partial_windows_take_the_accumulator_free_kernel(ctx, chunk):
+    """Peak and energy windows that cover only part of the run: steps outside
+    both windows run the paired kernel without accumulators (whole captured
+    chunks or single steps), and every output equals the one-cell kernel's,
+    which always carries the accumulators."""
+    res = {}
+    for v in (21, 17):
+        p = presets.cfg1(40, 40, 64, 230, precision=abi.BD_F32)
+        p.params.peak_start, p.params.peak_end = 50, 120
+        p.params.energy_start, p.params.energy_end = 100, 185
+        p.params.graph_chunk = chunk
+        p.params.tile_variant = v
+        res[v] = ctx.westervelt(p, want=("p_final", "peak", "energy"))
+    assert np.abs(res[21]["energy"]).max() > 0
+    for k in ("p_final", "peak", "energy"):
+        np.testing.assert_array_equal(res[21][k], res[17][k], err_msg=k)
