@@ -391,13 +391,13 @@ def cfg5_summary(ctx, n_steps=12000, n_bubbles=1 << 18, t_end=0.1e-6):
 
 
 def gilmore_summary(ctx, n=1 << 20, t_end=0.004e-6, cpu_n=1 << 14, with_cpu=True):
-    """cfg2 bubbles (all 2^20 by default) over a bounded window through three
-    kernels: the persistent work-stealing fast path, the same arithmetic one
-    thread per bubble (static), and the naive baseline: one thread per bubble
-    in the reference's operation order (7 right-hand sides with their pow calls
-    per attempt, G:212-318) at the same cfg2 settings (phases, rtol 1e-8).  The
-    CPU oracle runs the first cpu_n of them over the same window, all host
-    cores."""
+    """cfg2 bubbles (all 2^20 by default) over a bounded window through two
+    kernels: the persistent work-stealing fast path and the naive baseline,
+    one thread per bubble in the reference's operation order (7 right-hand
+    sides with their pow calls per attempt, G:212-318) at the same cfg2
+    settings (phases, rtol 1e-8).  The CPU oracle runs the first cpu_n of them
+    over the same window, all host cores.  (The fast arithmetic one thread per
+    bubble is `--workload gilmore --schedule static`.)"""
     import numpy as np
     from bubbledynamics_gb300 import abi, presets
     med = presets.cfg2_medium()
@@ -413,8 +413,7 @@ def gilmore_summary(ctx, n=1 << 20, t_end=0.004e-6, cpu_n=1 << 14, with_cpu=True
         out["cpu_baseline"] = {"bubbles_per_s": cpu_n / dt, "bubble_us_per_s": cpu_n * t_end * 1e6 / dt,
                                "cores": orc.threads(), "kind": "port",
                                "sample": "first %d bubbles, same window, FP64 oracle (OpenMP)" % cpu_n}
-    for name, sched, ref in (("persistent", abi.BD_SCHEDULE_PERSISTENT, 0), ("static", abi.BD_SCHEDULE_STATIC, 0),
-                             ("naive_static", abi.BD_SCHEDULE_STATIC, 1)):
+    for name, sched, ref in (("persistent", abi.BD_SCHEDULE_PERSISTENT, 0), ("naive_static", abi.BD_SCHEDULE_STATIC, 1)):
         o = presets.cfg2_ode(t_end=t_end)
         o.schedule = sched
         o.ref_arith = ref
@@ -425,7 +424,6 @@ def gilmore_summary(ctx, n=1 << 20, t_end=0.004e-6, cpu_n=1 << 14, with_cpu=True
         if name == "persistent":
             acc = r["n_accept"].astype(np.float64)
     out["accepted_steps"] = {"mean": float(acc.mean()), "max": float(acc.max())}
-    out["speedup_vs_static"] = out["static"]["ms"] / out["persistent"]["ms"]
     out["speedup_vs_naive_static"] = out["naive_static"]["ms"] / out["persistent"]["ms"]
     return out
 
@@ -500,6 +498,29 @@ def run_gilmore(args):
     ctx.close()
 
 
+def run_threshold_scale(args):
+    """G's threshold search over its whole table (27,775 combinations x 100
+    radii = 2,777,500 items, G:498-520, G:457-460, G:573) with every
+    integration capped at --max-steps accepted steps: every item climbs the
+    0.1 MPa ladder to 10 MPa, so the run measures the search kernel's attempt
+    rate and item coverage at the reference's scale (an uncapped search of the
+    table is about 1.7e13 attempts)."""
+    import numpy as np
+    from bubbledynamics_gb300 import api, presets
+    ctx = api.Context(0)
+    combos = api.gilmore_combos()
+    R0 = presets.ref_G_R0s()
+    A, ms = ctx.gilmore_threshold(presets.ref_G_medium(), combos, R0, ref_arith=0, max_steps=args.max_steps)
+    items = A.size
+    attempts_lower_bound = items * 100 * args.max_steps      # every ladder that climbs to 10 MPa
+    print(json.dumps({"workload": "G threshold search, whole table, integrations capped at %d steps" % args.max_steps,
+                      "items": int(items), "ms": ms, "items_per_s": items / (ms * 1e-3),
+                      "accepted_steps_per_s_lower_bound": attempts_lower_bound / (ms * 1e-3),
+                      "every_item_written": bool(np.all(A > 0)),
+                      "items_reaching_threshold_within_cap": int((A < 1e7).sum())}), flush=True)
+    ctx.close()
+
+
 def run_heat(args):
     """cfg3 heat steps on the 256x256x384 grid with a Gaussian focal source, one
     spot: the case the heat-kernel ncu captures run."""
@@ -569,7 +590,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference", "reference-gpu"])
     ap.add_argument("--workload", default="westervelt",
-                    choices=["westervelt", "step-kernel", "gilmore", "heat", "adjoint", "dft"])
+                    choices=["westervelt", "step-kernel", "gilmore", "heat", "adjoint", "dft", "threshold-scale"])
+    ap.add_argument("--max-steps", type=int, default=100, help="threshold-scale workload: step cap per integration")
     ap.add_argument("--bubbles", type=int, default=1 << 16, help="gilmore workload: bubbles")
     ap.add_argument("--t-end", type=float, default=2e-6, help="gilmore workload: window [s]")
     ap.add_argument("--schedule", default="persistent", choices=["persistent", "static"])
@@ -593,9 +615,10 @@ def main():
     elif args.workload == "step-kernel":
         if rank == 0:
             run_step_kernel(args)
-    elif args.workload in ("gilmore", "heat", "adjoint", "dft"):
+    elif args.workload in ("gilmore", "heat", "adjoint", "dft", "threshold-scale"):
         if rank == 0:
-            {"gilmore": run_gilmore, "heat": run_heat, "adjoint": run_adjoint, "dft": run_dft}[args.workload](args)
+            {"gilmore": run_gilmore, "heat": run_heat, "adjoint": run_adjoint, "dft": run_dft,
+             "threshold-scale": run_threshold_scale}[args.workload](args)
     else:
         run_westervelt(args, world, rank, local)
     if world > 1:

@@ -1183,7 +1183,8 @@ static void adjoint_solve(WvSession& S, const bd_focal_loss* loss, double* loss_
     // segment, the parity of its index (relaxation ring) and the number of
     // backward steps done modulo 6 (adjoint rings), and its index comes from a
     // device counter, so one graph per key serves every full segment.
-    const bool use_graphs = S.p.graph_chunk >= 0;
+    // (only when several segments share a graph: a graph used once costs its capture)
+    const bool use_graphs = S.p.graph_chunk >= 0 && N / Kc >= 3;
     struct GraphCache {
         std::map<int, cudaGraphExec_t> g;
         ~GraphCache() { for (auto& kv : g) cudaGraphExecDestroy(kv.second); }
