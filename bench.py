@@ -18,8 +18,10 @@ host (oracle/_ref) on the same grid (its two-layer physics), all host cores.
 --impl reference-gpu times the reference's own CUDA kernels (W's step loop,
 G's DPRK_step one thread per bubble; oracle/_ref/libbdref_gpu.so) beside this
 library on the same problems (the comparison baseline of the speed-ups).
-The default line also carries the cfg3, cfg4, cfg5 and cfg2 summaries
-(--no-extra skips them).
+The default line also carries the cfg3, cfg4, cfg5 and cfg2 summaries and
+the reference's own Westervelt kernels on the GPU (--no-extra skips them).
+--workload threshold-scale runs G's search over its whole table with capped
+integrations.
 --gpus N under torchrun: N independent replicas (the solver does not shard).
 """
 import argparse
@@ -43,7 +45,7 @@ UNIT = "Gcell-updates/s"
 # dram__bytes_read.sum + dram__bytes_write.sum of one step-kernel launch on the
 # cfg1 grid (first launch of the ncu capture of tile variant 21, the
 # wv_tma_pair_kernel the autotuner picks)
-NCU_TRAFFIC_BYTES = 202600192
+NCU_TRAFFIC_BYTES = 203221248
 
 
 def peaks():
@@ -282,6 +284,8 @@ def run_westervelt(args, world, rank, local):
         line["cfg3"] = cfg3_summary(ctx)
         line["cfg5"] = cfg5_summary(ctx)
         line["gilmore"] = gilmore_summary(ctx, with_cpu=not args.no_cpu)
+        # the reference's own W kernels built for this GPU, on the cfg1 grid with its physics
+        line["reference_gpu"] = reference_gpu_summary(ctx, gilmore=False)
     if rank == 0:
         print(json.dumps(line), flush=True)
     ctx.close()
@@ -390,7 +394,7 @@ def cfg5_summary(ctx, n_steps=12000, n_bubbles=1 << 18, t_end=0.1e-6):
     return out
 
 
-def gilmore_summary(ctx, n=1 << 20, t_end=0.004e-6, cpu_n=1 << 14, with_cpu=True):
+def gilmore_summary(ctx, n=1 << 20, t_end=0.004e-6, cpu_n=1 << 12, with_cpu=True):
     """cfg2 bubbles (all 2^20 by default) over a bounded window through two
     kernels: the persistent work-stealing fast path and the naive baseline,
     one thread per bubble in the reference's operation order (7 right-hand
@@ -428,7 +432,7 @@ def gilmore_summary(ctx, n=1 << 20, t_end=0.004e-6, cpu_n=1 << 14, with_cpu=True
     return out
 
 
-def reference_gpu_summary(ctx, w_steps=100, g_n=1 << 15, g_t_end=0.1e-6):
+def reference_gpu_summary(ctx, w_steps=100, g_n=1 << 15, g_t_end=0.1e-6, gilmore=True):
     """The reference's own CUDA kernels (oracle/_ref/libbdref_gpu.so) against
     this library on the same problems: W's step loop on the cfg1 grid with the
     reference's two-layer physics, and G's DPRK_step one thread per bubble on
@@ -462,6 +466,8 @@ def reference_gpu_summary(ctx, w_steps=100, g_n=1 << 15, g_t_end=0.1e-6):
     w["speedup_f64"] = ref_us / w["ours_f64_us_per_step"]
     w["speedup_f32"] = ref_us / w["ours_f32_us_per_step"]
     out["westervelt"] = w
+    if not gilmore:
+        return out
     # ---- Gilmore, one thread per bubble with G's DPRK_step
     med = presets.cfg2_medium()
     b = presets.cfg2_bubbles(1 << 20)[:g_n]

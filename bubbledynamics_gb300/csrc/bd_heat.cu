@@ -65,6 +65,16 @@ __device__ __forceinline__ float2 df_add(float2 d, float x) {
     return make_float2(hi, lo - (hi - s.x));
 }
 
+// A positive float widened to double with integer operations (exponent rebias,
+// mantissa shift), so the conversion stays off the FP64 pipe, which the dose
+// add already occupies; exact for normal floats, and values below the float
+// normal range (dose rates under 1e-38) become zero.
+__device__ __forceinline__ double widen_pos(float x) {
+    const int b = __float_as_int(x);
+    if (b < 0x00800000) return 0.0;                        // zero or subnormal
+    return __longlong_as_double(((long long)b << 29) + (896LL << 52));
+}
+
 template <class real>
 __global__ void heat_step_kernel(const HeatArgs<real> a, int koff) {
     const int ix = blockIdx.x * blockDim.x + threadIdx.x;
@@ -96,7 +106,7 @@ __global__ void heat_step_kernel(const HeatArgs<real> a, int koff) {
         } else {
             const float x = (float)tn + a.T_refm43;                    // T_C - 43
             const float inc = exp2f(x < 0.0f ? 2.0f * x : x) * (float)a.dt;
-            if (a.TD) a.TD[i] = a.TD[i] + (double)inc;
+            if (a.TD) a.TD[i] = a.TD[i] + widen_pos(inc);
             else a.TDf[i] = df_add(a.TDf[i], inc);
         }
     };
@@ -192,7 +202,7 @@ __global__ void __launch_bounds__(128) heat_step4_kernel(const HeatArgs<float> a
             if (upd[k]) {
                 const float x = t + a.T_refm43;                   // T_C - 43
                 const float inc = exp2f(x < 0.0f ? 2.0f * x : x) * a.dt;   // T:99-102
-                dose[k] = dose[k] + (double)inc;
+                dose[k] = dose[k] + widen_pos(inc);
             }
         }
         *reinterpret_cast<float4*>(a.Tout + i) = make_float4(tn[0], tn[1], tn[2], tn[3]);
