@@ -58,7 +58,25 @@ def test_slab_arguments_checked(ctx):
         ctx.westervelt_slab(p, 4, 20)         # the ghost planes would reach the z- Mur layers
     with pytest.raises(api.BDError):
         ctx.westervelt_slabs(p, 6)            # more slabs than nz / 8
+    torch = pytest.importorskip("torch")
     s = ctx.westervelt_slab(p, 0, 20)
-    with pytest.raises(api.BDError):
-        s.halo_copy(0, 0, 0)                  # side 0 of the first slab is the grid's face
+    buf = torch.empty(s.halo_bytes(), dtype=torch.uint8, device="cuda")
+    with pytest.raises(api.BDError) as ei:
+        s.halo_copy(0, 0, buf.data_ptr())     # side 0 of the first slab is the grid's face
+    assert ei.value.status == abi.BD_ERR_INVALID_ARG and "face of the grid" in str(ei.value)
+    s.halo_copy(1, 0, buf.data_ptr())         # side 1 is an internal face
     s.close()
+
+
+def test_slab_boundary_inside_the_dft_planes(ctx):
+    """cfg5 physics on a 64x64x96 box (two relaxation processes, three tones,
+    the 9-frequency DFT on planes 74..95) in five slabs, the last boundary at
+    plane 76 inside the DFT planes: every slab keeps its own part of the DFT
+    and the assembled maps equal the one-domain solve bit for bit."""
+    p = presets.cfg5(nx=64, ny=64, nz=96, n_steps=150, window_steps=60)
+    p.params.tile_variant = 21
+    assert p.params.dft_z_lo < 76 < p.params.dft_z_hi
+    one = ctx.westervelt(p, want=("p_final", "peak", "energy", "dft"))
+    many = ctx.westervelt_slabs(p, 5, want=("p_final", "peak", "energy", "dft"))
+    assert np.abs(one["dft_re"]).max() > 0
+    _equal(one, many, ("p_final", "peak", "energy", "dft_re", "dft_im"))
