@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define BD_ABI_VERSION 1
+#define BD_ABI_VERSION 2   /* 2: bd_thermal.plain_launches; z-slab entry points */
 
 #define BD_MAX_MATERIALS 8
 #define BD_MAX_RELAX 4

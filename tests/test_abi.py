@@ -26,7 +26,7 @@ def test_library_exports_every_declared_function(lib):
     assert len(names) >= 20
     missing = [n for n in names if not hasattr(lib, n)]
     assert missing == []
-    assert lib.bd_abi_version() == 1
+    assert lib.bd_abi_version() == 2
 
 
 def test_struct_layout_matches_c():
