@@ -87,6 +87,7 @@ struct WvSession {
     // adjoint: TMA map of the H buffer for the stencil pass (valid while adj_tma)
     CUtensorMap adj_mapH;
     bool adj_tma = false;
+    bool adj_fused = false;     // adjoint: one fused pass per backward step (FP32, nx % 4 == 0)
     CUtensorMap mP0[5], mQ[5], mR[BD_MAX_RELAX][2], mC, mPeak, mEnergy;
     // segment view (TMA variants only): the pressure levels of the next step are
     // read from, and p^{n+1} written to, caller-chosen buffers instead of the ring
@@ -1083,6 +1084,14 @@ template <class real, int NR>
 static void adj_launch_n(WvSession& S, const AdjArgs<real>& a, cudaStream_t st) {
     const WvConst<real>* K = S.kconst.as<WvConst<real>>();
     constexpr int VEC = 16 / sizeof(real);
+    if constexpr (sizeof(real) == 4) {
+        if (S.adj_fused) {
+            const long long nv = (long long)S.ncell / 4;
+            adj_point_kernel<real, NR, 4, true><<<(unsigned)((nv + 255) / 256), 256, 0, st>>>(a, K);
+            BD_LAUNCHED(S.ctx);
+            return;
+        }
+    }
     if (S.nx % VEC == 0) {
         const long long nv = (long long)S.ncell / VEC;
         adj_point_kernel<real, NR, VEC><<<(unsigned)((nv + 255) / 256), 256, 0, st>>>(a, K);
@@ -1285,15 +1294,20 @@ static void adjoint_solve(WvSession& S, const bd_focal_loss* loss, double* loss_
             }
     if (loss_out) *loss_out = L;
     // backward buffers
-    PoolBuf mu[6], muR[BD_MAX_RELAX][3], gphi, gamp, eamp, H;
-    H.alloc(S.ctx, f);
-    // FP32 stencil pass with TMA-streamed H planes where the row pitch allows it
-    S.adj_tma = S.prec == BD_F32 && tma_eligible(S);
-    if (S.adj_tma) S.adj_mapH = make_map(S, H.p, true, 64 + 8, 8 + 6);
+    PoolBuf mu[6], muR[BD_MAX_RELAX][3], gphi, gamp, eamp, Hb[2];
+    // FP32 grids with nx % 4 == 0 fold the stencil pass into the next step's
+    // pointwise pass (H alternates between two buffers by the parity of s);
+    // the others run the two passes, the stencil pass with TMA-streamed H
+    // planes where the row pitch allows it
+    S.adj_fused = S.prec == BD_F32 && S.nx % 4 == 0;
+    for (auto& b : Hb) { b.alloc(S.ctx, f); BD_CUDA(cudaMemsetAsync(b.p, 0, f, st)); }
+    S.adj_tma = !S.adj_fused && S.prec == BD_F32 && tma_eligible(S);
+    if (S.adj_tma) S.adj_mapH = make_map(S, Hb[0].p, true, 64 + 8, 8 + 6);
     struct AdjTmaOff {
         WvSession& s;
-        ~AdjTmaOff() { s.adj_tma = false; }
+        ~AdjTmaOff() { s.adj_tma = false; s.adj_fused = false; }
     } adj_tma_off{S};
+    const int per_step = S.adj_fused ? 1 : 2;     // kernels per backward step
     for (auto& b : mu) { b.alloc(S.ctx, f); BD_CUDA(cudaMemsetAsync(b.p, 0, f, st)); }
     for (int v = 0; v < S.max_relax; ++v)
         for (auto& b : muR[v]) { b.alloc(S.ctx, f); BD_CUDA(cudaMemsetAsync(b.p, 0, f, st)); }
@@ -1337,7 +1351,8 @@ static void adjoint_solve(WvSession& S, const bd_focal_loss* loss, double* loss_
         const long long tiles = (long long)((S.nx + 31) / 32) * ((S.ny + 7) / 8);
         const long long target = 32LL * S.ctx->sm_count;
         a.zb = (int)std::min<long long>(64, std::max<long long>(4, (tiles * S.nz + target - 1) / target));
-        a.H = H.as<real>();
+        a.H = Hb[0].as<real>();
+        a.Hin = Hb[1].as<real>();
     }
     a.gphi = gphi.as<double>(); a.gamp = gamp.as<double>(); a.e_amp = eamp.as<double>();
     a.sAf = S.sAf.as<float>(); a.sPsi = S.sPsi.as<float>(); a.sTauf = S.sTauf.as<float>();
@@ -1378,6 +1393,10 @@ static void adjoint_solve(WvSession& S, const bd_focal_loss* loss, double* loss_
                 a.muR3[v] = muR[v][(rrot + 2) % 3].as<real>();
             }
             for (int k = 0; k < 5; ++k) a.fp[k] = seg[s - s0 + 5 - k].as<real>();
+            if (S.adj_fused) {
+                a.H = Hb[s & 1].as<real>();            // written by this step
+                a.Hin = Hb[(s + 1) & 1].as<real>();    // written by step s + 1 (zero before the first)
+            }
             a.koff = koff;
             adj_launch<real>(S, a, cs);
             rot = (rot + 1) % 6;      // lambda_k now sits in the buffer of mu_{k+1}, lambda_4 in the spare
@@ -1403,7 +1422,8 @@ static void adjoint_solve(WvSession& S, const bd_focal_loss* loss, double* loss_
         BD_CUDA(cudaEventRecord(S.ctx->ev1, st));
         if (use_graphs && s1 - s0 == Kc) {
             const int64_t nb = nb_done;
-            captured(bwd_graphs, (int)(nb % 6), 2 * Kc + 1, [&](cudaStream_t cs) { backward_steps(cs, s0, s1, nb); });
+            captured(bwd_graphs, (int)(nb % 6), per_step * Kc + 1,
+                     [&](cudaStream_t cs) { backward_steps(cs, s0, s1, nb); });
         } else {
             backward_steps(st, s0, s1, nb_done);
         }

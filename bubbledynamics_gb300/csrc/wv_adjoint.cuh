@@ -37,7 +37,8 @@ struct AdjArgs {
     // forward fields: fp[0] = p^{s+1}, fp[1] = p^s, fp[2] = p^{s-1}, fp[3] = p^{s-2}, fp[4] = p^{s-3}
     const real* fp[5];
     int zb;                     // z planes per CTA of the stencil pass
-    real* H;                    // c^2 (adjoint of Y)
+    real* H;                    // c^2 (adjoint of Y) of this backward step
+    const real* Hin;            // H of the later backward step (fused pass: its stencil term completes mu_0)
     const float* cmap;
     const uint8_t* matmap;
     const int* plane_mat;
@@ -239,9 +240,51 @@ __device__ __forceinline__ void vstore(real* p, const Vec<real, VEC>& r) {
     }
 }
 
+// The transposed 6th-order stencil of H (zero outside the grid) at four
+// consecutive x cells (x0 % 4 == 0, nx % 4 == 0), added to lin:
+// lin + kxy180 (Sxx + Syy) + kz180 Szz in the stencil pass's operation order.
+__device__ __forceinline__ void add_stencil4(const AdjArgs<float>& a, const float* __restrict__ H, long long col,
+                                             int x0, int iy, int iz, float* lin) {
+    const long long nx = a.nx;
+    auto row = [&](int z, int dy) -> float4 {
+        const int y = iy + dy;
+        if (z < 0 || z >= a.nz || y < 0 || y >= a.ny) return make_float4(0.f, 0.f, 0.f, 0.f);
+        return __ldg(reinterpret_cast<const float4*>(H + (long long)z * a.plane + col + (long long)dy * nx));
+    };
+    const float* P = H + (long long)iz * a.plane + col;
+    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 c4 = row(iz, 0);
+    const float4 Lq = x0 >= 4 ? __ldg(reinterpret_cast<const float4*>(P - 4)) : zero;
+    const float4 Rq = x0 + 4 < a.nx ? __ldg(reinterpret_cast<const float4*>(P + 4)) : zero;
+    const float4 yp1 = row(iz, 1), ym1 = row(iz, -1), yp2 = row(iz, 2), ym2 = row(iz, -2), yp3 = row(iz, 3),
+                 ym3 = row(iz, -3);
+    const float4 zp1 = row(iz + 1, 0), zm1 = row(iz - 1, 0), zp2 = row(iz + 2, 0), zm2 = row(iz - 2, 0),
+                 zp3 = row(iz + 3, 0), zm3 = row(iz - 3, 0);
+    const float xs[12] = {Lq.x, Lq.y, Lq.z, Lq.w, c4.x, c4.y, c4.z, c4.w, Rq.x, Rq.y, Rq.z, Rq.w};
+    const float y1[4] = {yp1.x + ym1.x, yp1.y + ym1.y, yp1.z + ym1.z, yp1.w + ym1.w};
+    const float y2[4] = {yp2.x + ym2.x, yp2.y + ym2.y, yp2.z + ym2.z, yp2.w + ym2.w};
+    const float y3[4] = {yp3.x + ym3.x, yp3.y + ym3.y, yp3.z + ym3.z, yp3.w + ym3.w};
+    const float z1[4] = {zp1.x + zm1.x, zp1.y + zm1.y, zp1.z + zm1.z, zp1.w + zm1.w};
+    const float z2[4] = {zp2.x + zm2.x, zp2.y + zm2.y, zp2.z + zm2.z, zp2.w + zm2.w};
+    const float z3[4] = {zp3.x + zm3.x, zp3.y + zm3.y, zp3.z + zm3.z, zp3.w + zm3.w};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const float ax1 = xs[5 + k] + xs[3 + k], ax2 = xs[6 + k] + xs[2 + k], ax3 = xs[7 + k] + xs[1 + k];
+        const float h0 = xs[4 + k];
+        const float sxy = -980.f * h0 + 270.f * (ax1 + y1[k]) - 27.f * (ax2 + y2[k]) + 2.f * (ax3 + y3[k]);
+        const float sz = -490.f * h0 + 270.f * z1[k] - 27.f * z2[k] + 2.f * z3[k];
+        lin[k] = lin[k] + a.kxy180 * sxy + a.kz180 * sz;
+    }
+}
+
 // Pointwise pass.  Thread = VEC consecutive cells along x (nx % VEC == 0).
-template <class real, int NRMAX, int VEC>
+// FUSE (FP32, VEC = 4): the stencil pass of the later step is folded in: mu_0
+// arrives without its stencil term, which is added here from that step's H
+// (a.Hin), and lambda_0 is left without its own, which the next step adds;
+// one kernel per backward step and no lambda_0 round trip.
+template <class real, int NRMAX, int VEC, bool FUSE = false>
 __global__ void __launch_bounds__(256) adj_point_kernel(const AdjArgs<real> a, const WvConst<real>* __restrict__ Kp) {
+    static_assert(!FUSE || (VEC == 4 && sizeof(real) == 4), "the fused pass takes four FP32 cells per thread");
     __shared__ MatConst<real> sM[BD_MAX_MATERIALS];
     {
         const int n = (int)(sizeof(sM) / sizeof(int));
@@ -258,6 +301,7 @@ __global__ void __launch_bounds__(256) adj_point_kernel(const AdjArgs<real> a, c
     const int iy = (int)(col0 / a.nx), ix0 = (int)(col0 - (long long)iy * a.nx);
     const long long step = adj_step(a);
     Vec<real, VEC> m0 = vload<real, VEC>(a.mu[0] + i0);
+    if constexpr (FUSE) add_stencil4(a, a.Hin, col0, ix0, iy, iz, m0.v);
     Vec<real, VEC> l0 = vload<real, VEC>(a.mu[1] + i0);
     Vec<real, VEC> l1 = vload<real, VEC>(a.mu[2] + i0);
     Vec<real, VEC> l2 = vload<real, VEC>(a.mu[3] + i0);
