@@ -84,9 +84,6 @@ struct WvSession {
     int graph_variant[2] = {-1, -1};
     // tensor maps of the TMA variant in use (built per tile shape)
     int maps_tx = 0, maps_ty = 0;
-    // adjoint: TMA map of the H buffer for the stencil pass (valid while adj_tma)
-    CUtensorMap adj_mapH;
-    bool adj_tma = false;
     bool adj_fused = false;     // adjoint: one fused pass per backward step (FP32, nx % 4 == 0)
     CUtensorMap mP0[5], mQ[5], mR[BD_MAX_RELAX][2], mC, mPeak, mEnergy;
     // segment view (TMA variants only): the pressure levels of the next step are
@@ -1099,42 +1096,6 @@ static void adj_launch_n(WvSession& S, const AdjArgs<real>& a, cudaStream_t st) 
         adj_point_kernel<real, NR, 1><<<(unsigned)((S.ncell + 255) / 256), 256, 0, st>>>(a, K);
     }
     BD_LAUNCHED(S.ctx);
-    if constexpr (sizeof(real) == 4) {
-        if (S.adj_tma) {
-            // H planes streamed by TMA, z-chunk fitted to whole waves of resident CTAs
-            // (on cfg4 this pass takes 25 us of the 106 us backward step; the pointwise
-            // pass streams at 0.91 of HBM)
-            constexpr int TX = 64, TY = 8, NPA = 8;
-            using LA = AdjTmaLayout<TX, TY, NPA>;
-            static int per_sm = 0;
-            if (!per_sm) {
-                BD_CUDA(cudaFuncSetAttribute(adj_stencil_tma_kernel<TX, TY, NPA>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, LA::SMEM));
-                BD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, adj_stencil_tma_kernel<TX, TY, NPA>,
-                                                                      TX * TY / 2, LA::SMEM));
-            }
-            AdjArgs<real> at = a;
-            const long long tiles = (long long)((S.nx + TX - 1) / TX) * ((S.ny + TY - 1) / TY);
-            // fewer, longer chunks: each chunk first fills its six-plane z window
-            at.zb = wave_fitted_zb(tiles, S.nz, (long long)S.ctx->sm_count * std::max(per_sm, 1), 0.9, true);
-            dim3 b(TX / 2, TY), g((S.nx + TX - 1) / TX, (S.ny + TY - 1) / TY, (S.nz + at.zb - 1) / at.zb);
-            adj_stencil_tma_kernel<TX, TY, NPA><<<g, b, LA::SMEM, st>>>(at, S.adj_mapH, S.flag.as<unsigned>() + 1);
-            BD_LAUNCHED(S.ctx);
-            return;
-        }
-        if (S.nx % 4 == 0) {
-            // z-chunk fitted to whole waves of the four-cell kernel's resident CTAs
-            static int per_sm = 0;
-            if (!per_sm) BD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, adj_stencil4_kernel, 128, 0));
-            AdjArgs<real> a4 = a;
-            const long long tiles = (long long)((S.nx / 4 + 15) / 16) * ((S.ny + 7) / 8);
-            a4.zb = wave_fitted_zb(tiles, S.nz, (long long)S.ctx->sm_count * std::max(per_sm, 1), 0.9);
-            dim3 b(16, 8), g((S.nx / 4 + 15) / 16, (S.ny + 7) / 8, (S.nz + a4.zb - 1) / a4.zb);
-            adj_stencil4_kernel<<<g, b, 0, st>>>(a4);
-            BD_LAUNCHED(S.ctx);
-            return;
-        }
-    }
     dim3 b(32, 8), g((S.nx + 31) / 32, (S.ny + 7) / 8, (S.nz + a.zb - 1) / a.zb);
     adj_stencil_kernel<real><<<g, b, 0, st>>>(a);
     BD_LAUNCHED(S.ctx);
@@ -1159,10 +1120,11 @@ static void adjoint_solve(WvSession& S, const bd_focal_loss* loss, double* loss_
     const int64_t sqrtN = std::max<int64_t>(1, (int64_t)std::ceil(std::sqrt((double)N)));
     int64_t Kc = loss->checkpoint_every > 0 ? std::min<int64_t>(loss->checkpoint_every, N) : sqrtN;
     if (loss->checkpoint_every < 0) {
-        // the whole history when it fits in half of the free device memory
+        // the whole history when it fits in half of the free device memory; blocks
+        // the context's pool holds from earlier solves count as free (they are reused)
         size_t fr = 0, tot = 0;
         BD_CUDA(cudaMemGetInfo(&fr, &tot));
-        if ((double)(N + 5) * (double)f <= 0.5 * (double)fr) Kc = N;
+        if ((double)(N + 5) * (double)f <= 0.5 * ((double)fr + (double)S.ctx->pool_bytes)) Kc = N;
     }
     const int64_t nck = (N + Kc - 1) / Kc;
     const int nlev = 5 + 2 * S.max_relax;
@@ -1297,16 +1259,13 @@ static void adjoint_solve(WvSession& S, const bd_focal_loss* loss, double* loss_
     PoolBuf mu[6], muR[BD_MAX_RELAX][3], gphi, gamp, eamp, Hb[2];
     // FP32 grids with nx % 4 == 0 fold the stencil pass into the next step's
     // pointwise pass (H alternates between two buffers by the parity of s);
-    // the others run the two passes, the stencil pass with TMA-streamed H
-    // planes where the row pitch allows it
+    // the others run the pointwise and stencil passes
     S.adj_fused = S.prec == BD_F32 && S.nx % 4 == 0;
     for (auto& b : Hb) { b.alloc(S.ctx, f); BD_CUDA(cudaMemsetAsync(b.p, 0, f, st)); }
-    S.adj_tma = !S.adj_fused && S.prec == BD_F32 && tma_eligible(S);
-    if (S.adj_tma) S.adj_mapH = make_map(S, Hb[0].p, true, 64 + 8, 8 + 6);
-    struct AdjTmaOff {
+    struct AdjFusedOff {
         WvSession& s;
-        ~AdjTmaOff() { s.adj_tma = false; s.adj_fused = false; }
-    } adj_tma_off{S};
+        ~AdjFusedOff() { s.adj_fused = false; }
+    } adj_fused_off{S};
     const int per_step = S.adj_fused ? 1 : 2;     // kernels per backward step
     for (auto& b : mu) { b.alloc(S.ctx, f); BD_CUDA(cudaMemsetAsync(b.p, 0, f, st)); }
     for (int v = 0; v < S.max_relax; ++v)

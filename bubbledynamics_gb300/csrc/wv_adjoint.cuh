@@ -7,13 +7,16 @@
 //   lambda_k = mu_{k+1} + (d p^{s+1} / d p^{s-k})^T mu_0 + (d R^s / d p^{s-k})^T muR1
 // The loss is sum_x w_L(x) sum_{s in window} p^{s+1}(x)^2 dt.
 //
-// Two kernels per backward step.  The pointwise pass reads only its own cell
-// (16-byte vector loads, several cells per thread): it adds the loss term,
-// forms gY, gD, gE and the relaxation adjoints, writes lambda_1..lambda_4, the
-// relaxation adjoints, lambda_0 without the stencil term, and H = c^2 gY.  The
-// stencil pass then adds the transposed 6th-order Laplacian of H to lambda_0.
-// lambda_4 goes to a spare buffer (the adjoint ring has six) and the
-// relaxation adjoints rotate through three buffers per process.
+// The pointwise pass reads only its own cell (16-byte vector loads, several
+// cells per thread): it adds the loss term, forms gY, gD, gE and the
+// relaxation adjoints, writes lambda_1..lambda_4, the relaxation adjoints,
+// lambda_0 without the stencil term, and H = c^2 gY.  The transposed 6th-order
+// Laplacian of H still has to be added to lambda_0: FP32 grids with nx % 4 == 0
+// do it in the next backward step's pointwise pass, as that pass loads lambda_0
+// as its mu_0 (one kernel per step); the others run a stencil pass after the
+// pointwise one (two kernels per step).  lambda_4 goes to a spare buffer (the
+// adjoint ring has six) and the relaxation adjoints rotate through three
+// buffers per process.
 #pragma once
 
 #include "wv_tma.cuh"
@@ -283,7 +286,7 @@ __device__ __forceinline__ void add_stencil4(const AdjArgs<float>& a, const floa
 // (a.Hin), and lambda_0 is left without its own, which the next step adds;
 // one kernel per backward step and no lambda_0 round trip.
 template <class real, int NRMAX, int VEC, bool FUSE = false>
-__global__ void __launch_bounds__(256) adj_point_kernel(const AdjArgs<real> a, const WvConst<real>* __restrict__ Kp) {
+__global__ void __launch_bounds__(256, FUSE ? 4 : 1) adj_point_kernel(const AdjArgs<real> a, const WvConst<real>* __restrict__ Kp) {
     static_assert(!FUSE || (VEC == 4 && sizeof(real) == 4), "the fused pass takes four FP32 cells per thread");
     __shared__ MatConst<real> sM[BD_MAX_MATERIALS];
     {
@@ -458,188 +461,6 @@ __global__ void __launch_bounds__(256) adj_stencil_kernel(const AdjArgs<real> a)
         real a1, a2, a3;
         sxy(iz, a1, a2, a3);
         upd(iz, w, a1, a2, a3, lam[(long long)iz * a.plane + col]);
-    }
-}
-
-// The stencil pass on four consecutive x cells per thread (FP32, nx % 4 == 0):
-// every neighbour row comes as one 16-byte load — the row itself and the rows
-// 4 cells left and right for the x neighbours, six rows for y, one new plane
-// for z — instead of thirteen scalar loads per cell.
-__device__ __forceinline__ float4 ld4(const float* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
-__device__ __forceinline__ float4 add4(float4 a, float4 b) { return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
-
-__global__ void __launch_bounds__(128) adj_stencil4_kernel(const AdjArgs<float> a) {
-    const int x0 = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
-    const int iy = blockIdx.y * blockDim.y + threadIdx.y;
-    if (x0 >= a.nx || iy >= a.ny) return;
-    const int z0 = blockIdx.z * a.zb;
-    const int z1 = min(a.nz, z0 + a.zb);
-    const long long col = (long long)iy * a.nx + x0;
-    const float* __restrict__ H = a.H;
-    float* __restrict__ lam = a.mu[1];
-    const long long nx = a.nx;
-    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
-    auto row = [&](int z, int dy) -> float4 {
-        const int y = iy + dy;
-        if (z < 0 || z >= a.nz || y < 0 || y >= a.ny) return zero;
-        return ld4(H + (long long)z * a.plane + col + (long long)dy * nx);
-    };
-    float4 w[7];
-#pragma unroll
-    for (int k = 0; k < 6; ++k) w[k] = row(z0 - 3 + k, 0);
-    for (int iz = z0; iz < z1; ++iz) {
-        w[6] = row(iz + 3, 0);
-        const float* P = H + (long long)iz * a.plane + col;
-        const float4 Lq = x0 >= 4 ? ld4(P - 4) : zero;
-        const float4 Rq = x0 + 4 < a.nx ? ld4(P + 4) : zero;
-        const float4 y1 = add4(row(iz, 1), row(iz, -1));
-        const float4 y2 = add4(row(iz, 2), row(iz, -2));
-        const float4 y3 = add4(row(iz, 3), row(iz, -3));
-        const long long i = (long long)iz * a.plane + col;
-        float4 l = *reinterpret_cast<const float4*>(lam + i);
-        // x values x0-4 .. x0+7
-        const float xs[12] = {Lq.x, Lq.y, Lq.z, Lq.w, w[3].x, w[3].y, w[3].z, w[3].w, Rq.x, Rq.y, Rq.z, Rq.w};
-        const float c[4] = {w[3].x, w[3].y, w[3].z, w[3].w};
-        const float ys1[4] = {y1.x, y1.y, y1.z, y1.w}, ys2[4] = {y2.x, y2.y, y2.z, y2.w}, ys3[4] = {y3.x, y3.y, y3.z, y3.w};
-        const float zp1[4] = {w[4].x, w[4].y, w[4].z, w[4].w}, zm1[4] = {w[2].x, w[2].y, w[2].z, w[2].w};
-        const float zp2[4] = {w[5].x, w[5].y, w[5].z, w[5].w}, zm2[4] = {w[1].x, w[1].y, w[1].z, w[1].w};
-        const float zp3[4] = {w[6].x, w[6].y, w[6].z, w[6].w}, zm3[4] = {w[0].x, w[0].y, w[0].z, w[0].w};
-        float out[4] = {l.x, l.y, l.z, l.w};
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const float ax1 = xs[5 + k] + xs[3 + k], ax2 = xs[6 + k] + xs[2 + k], ax3 = xs[7 + k] + xs[1 + k];
-            const float h0 = c[k];
-            const float sxy = -980.f * h0 + 270.f * (ax1 + ys1[k]) - 27.f * (ax2 + ys2[k]) + 2.f * (ax3 + ys3[k]);
-            const float sz = -490.f * h0 + 270.f * (zp1[k] + zm1[k]) - 27.f * (zp2[k] + zm2[k]) + 2.f * (zp3[k] + zm3[k]);
-            out[k] = out[k] + a.kxy180 * sxy + a.kz180 * sz;
-        }
-        *reinterpret_cast<float4*>(lam + i) = make_float4(out[0], out[1], out[2], out[3]);
-#pragma unroll
-        for (int k = 0; k < 6; ++k) w[k] = w[k + 1];
-    }
-}
-
-// The same stencil pass with the H planes streamed by TMA: a CTA owns TX x TY
-// columns (two adjacent x cells per thread) and a z-chunk; one elected thread
-// keeps a ring of ADJ_NP (>= 7) plane tiles of H with their halo ((TX+8) x (TY+6),
-// x from 4 cells left of the block so the TMA x coordinate stays 16-byte
-// aligned; out-of-grid cells arrive as zeros, the stencil's ghost value) up to
-// ADJ_NP - 4 planes ahead, threads keep H(iz-3..iz+3) of their cells in registers,
-// and lambda_0 is read and written as one 8-byte pair per thread.  Needs a
-// row pitch that is a multiple of 16 bytes (nx % 4 == 0).  Waits are bounded
-// (bit 4 of *err, as in the forward kernels).
-template <int TX, int TY, int ADJ_NP = 8>
-struct AdjTmaLayout {
-    static constexpr int PW = TX + 8, PH = TY + 6;
-    static constexpr int PSLOT = ((PW * PH * 4 + 127) / 128) * 128;
-    static constexpr int SMEM = ADJ_NP * PSLOT + ADJ_NP * 8;
-};
-
-template <int TX, int TY, int ADJ_NP = 8>
-__global__ void __launch_bounds__(TX* TY / 2, 4) adj_stencil_tma_kernel(const AdjArgs<float> a,
-                                                                        const __grid_constant__ CUtensorMap mapH,
-                                                                        unsigned* __restrict__ err) {
-    using L = AdjTmaLayout<TX, TY, ADJ_NP>;
-    constexpr int TXT = TX / 2;
-    extern __shared__ __align__(128) unsigned char smem[];
-    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + ADJ_NP * L::PSLOT);
-    const int tx = threadIdx.x, ty = threadIdx.y;
-    const int tid = ty * TXT + tx;
-    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
-    const int z0 = blockIdx.z * a.zb;
-    const int z1 = min(a.nz, z0 + a.zb);
-    const int zbn = z1 - z0;
-    auto slot = [&](int q) { return reinterpret_cast<const float*>(smem + (q % ADJ_NP) * L::PSLOT); };
-    auto issue = [&](int q) {                      // plane z0 - 3 + q of H
-        if (q > zbn + 5) return;
-        const int plane = z0 - 3 + q;
-        uint64_t* b = &bar[q % ADJ_NP];
-        if (plane < 0 || plane >= a.nz) { mbar_arrive(b); return; }   // read as zeros, nothing to copy
-        mbar_expect_tx(b, L::PW * L::PH * 4u);
-        tma_load_3d(smem + (q % ADJ_NP) * L::PSLOT, &mapH, b, x0 - 4, y0 - 3, plane);
-    };
-    auto wait = [&](int q) { mbar_wait(&bar[q % ADJ_NP], (unsigned)((q / ADJ_NP) & 1), err); };
-    if (tid == 0) {
-        for (int s = 0; s < ADJ_NP; ++s) mbar_init(&bar[s], 1);
-        mbar_fence_init();
-    }
-    __syncthreads();
-    if (tid == 0)
-        for (int q = 0; q < ADJ_NP; ++q) issue(q);
-    const int lx = 2 * tx;
-    const int ix = x0 + lx, iy = y0 + ty;
-    const bool active = ix < a.nx && iy < a.ny;
-    const int own = (ty + 3) * L::PW + lx + 4;
-    const long long col = (long long)iy * a.nx + ix;
-    float w[2][7];
-#pragma unroll
-    for (int k = 0; k < 6; ++k) {                  // planes z0-3 .. z0+2
-        wait(k);
-        const int plane = z0 - 3 + k;
-        const bool in = plane >= 0 && plane < a.nz;
-        const float2 v = *reinterpret_cast<const float2*>(slot(k) + own);
-        w[0][k] = in ? v.x : 0.f;
-        w[1][k] = in ? v.y : 0.f;
-    }
-    __syncthreads();                               // slots of planes z0-3 .. z0-1 are free again
-    if (tid == 0)
-        for (int q = ADJ_NP; q < ADJ_NP + 3; ++q) issue(q);
-    // lambda_0 is read two planes ahead (registers), so its latency overlaps two planes of work
-    float* const lam0 = a.mu[1] + col;
-    auto lam_at = [&](int z) -> float2 {
-        return (active && z < z1) ? *reinterpret_cast<const float2*>(lam0 + (long long)z * a.plane)
-                                  : make_float2(0.f, 0.f);
-    };
-    float2 lnext[2] = {lam_at(z0), lam_at(z0 + 1)};
-    for (int iz = z0; iz < z1; ++iz) {
-        const int qc = iz - z0 + 3;
-        float* lam = lam0 + (long long)iz * a.plane;
-        const float2 l = lnext[0];
-        lnext[0] = lnext[1];
-        lnext[1] = lam_at(iz + 2);
-        wait(qc + 3);
-        {
-            const bool in = iz + 3 < a.nz;
-            const float2 v = *reinterpret_cast<const float2*>(slot(qc + 3) + own);
-            w[0][6] = in ? v.x : 0.f;
-            w[1][6] = in ? v.y : 0.f;
-        }
-        if (active) {
-            const float* c0 = slot(qc) + own;
-            constexpr int W = L::PW;
-            float xs[10];                          // x offsets -4 .. +5 from the first cell
-#pragma unroll
-            for (int j = 0; j < 5; ++j) {
-                const float2 v = *reinterpret_cast<const float2*>(c0 - 4 + 2 * j);
-                xs[2 * j] = v.x;
-                xs[2 * j + 1] = v.y;
-            }
-            float yp[3][2], ym[3][2];
-#pragma unroll
-            for (int j = 0; j < 3; ++j) {
-                const float2 u = *reinterpret_cast<const float2*>(c0 + (j + 1) * W);
-                const float2 v = *reinterpret_cast<const float2*>(c0 - (j + 1) * W);
-                yp[j][0] = u.x; yp[j][1] = u.y;
-                ym[j][0] = v.x; ym[j][1] = v.y;
-            }
-            const float lin[2] = {l.x, l.y};
-            float out[2];
-#pragma unroll
-            for (int k = 0; k < 2; ++k) {
-                const float ax1 = xs[5 + k] + xs[3 + k], ax2 = xs[6 + k] + xs[2 + k], ax3 = xs[7 + k] + xs[1 + k];
-                const float h0 = w[k][3];
-                const float sxy = -980.f * h0 + 270.f * (ax1 + (yp[0][k] + ym[0][k])) -
-                                  27.f * (ax2 + (yp[1][k] + ym[1][k])) + 2.f * (ax3 + (yp[2][k] + ym[2][k]));
-                const float sz = -490.f * h0 + 270.f * (w[k][4] + w[k][2]) - 27.f * (w[k][5] + w[k][1]) +
-                                 2.f * (w[k][6] + w[k][0]);
-                out[k] = lin[k] + a.kxy180 * sxy + a.kz180 * sz;
-            }
-            *reinterpret_cast<float2*>(lam) = make_float2(out[0], out[1]);
-        }
-#pragma unroll
-        for (int k = 0; k < 6; ++k) { w[0][k] = w[0][k + 1]; w[1][k] = w[1][k + 1]; }
-        __syncthreads();                           // plane qc's slot is free
-        if (tid == 0) issue(qc + ADJ_NP);
     }
 }
 
