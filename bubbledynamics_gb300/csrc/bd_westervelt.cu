@@ -85,7 +85,8 @@ struct WvSession {
     // tensor maps of the TMA variant in use (built per tile shape)
     int maps_tx = 0, maps_ty = 0;
     bool adj_fused = false;     // adjoint: one fused pass per backward step (FP32, nx % 4 == 0)
-    CUtensorMap mP0[5], mQ[5], mR[BD_MAX_RELAX][2], mC, mPeak, mEnergy;
+    CUtensorMap mP0[5], mQ[5], mR[BD_MAX_RELAX][2], mC, mPeak, mEnergy, mMat;
+    bool mat_tile = false;      // the material map travels as a TMA tile (nx % 16 == 0)
     // segment view (TMA variants only): the pressure levels of the next step are
     // read from, and p^{n+1} written to, caller-chosen buffers instead of the ring
     bool pdl = true;            // launch TMA step kernels with programmatic dependent launch
@@ -191,6 +192,7 @@ static WvArgs<real> make_args(WvSession& S, int64_t s) {
     a.energy_mode = S.p.energy_mode;
     a.n_dft = S.n_dft; a.dz_lo = S.dz_lo; a.dz_hi = S.dz_hi;
     a.relax_scheme = S.p.relax_scheme;
+    a.mat_tile = S.mat_tile ? 1 : 0;
     return a;
 }
 
@@ -206,14 +208,17 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
     return fn;
 }
 
-static CUtensorMap make_map(const WvSession& S, const void* base, bool is_float, int bx, int by) {
+static CUtensorMap make_map(const WvSession& S, const void* base, bool is_float, int bx, int by,
+                            bool is_u8 = false) {
     CUtensorMap m;
-    const size_t esz = is_float ? 4 : 8;
+    const size_t esz = is_u8 ? 1 : is_float ? 4 : 8;
     cuuint64_t dims[3] = {(cuuint64_t)S.nx, (cuuint64_t)S.ny, (cuuint64_t)S.nz};
     cuuint64_t strides[2] = {(cuuint64_t)S.nx * esz, (cuuint64_t)S.nx * S.ny * esz};
     cuuint32_t box[3] = {(cuuint32_t)bx, (cuuint32_t)by, 1};
     cuuint32_t estr[3] = {1, 1, 1};
-    CUresult r = encode_fn()(&m, is_float ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3,
+    const CUtensorMapDataType ty = is_u8 ? CU_TENSOR_MAP_DATA_TYPE_UINT8
+                                   : is_float ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
+    CUresult r = encode_fn()(&m, ty, 3,
                              const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
                              CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
@@ -244,6 +249,7 @@ static void build_maps(WvSession& S, int tx, int ty) {
     S.mPeak = make_map(S, S.peak.p, f, tx, ty);
     S.mEnergy = make_map(S, S.energy.p, f, tx, ty);
     if (S.has_cmap) S.mC = make_map(S, S.cmap.p, true, tx, ty);
+    if (S.mat_tile) S.mMat = make_map(S, S.matmap.p, false, tx, ty, true);
     S.maps_tx = tx;
     S.maps_ty = ty;
 }
@@ -309,6 +315,7 @@ static void step_maps(WvSession& S, int64_t s, int tx, int ty, TmaMaps& maps) {
     maps.peak = S.mPeak;
     maps.energy = S.mEnergy;
     if (S.has_cmap) maps.cmap = S.mC;
+    if (S.mat_tile) maps.mat = S.mMat;
 }
 
 template <class real, int TX, int TY, int CPT, int ZU>
@@ -694,6 +701,9 @@ static void setup(WvSession& S, bd_context* ctx, const bd_grid* g, const bd_medi
     S.has_cmap = m->c_map != nullptr;
     S.has_matmap = m->material_map != nullptr;
     S.has_planemat = m->plane_material != nullptr;
+    // the paired kernel takes the material map as a uint8 TMA tile when its rows
+    // (nx bytes) are a multiple of 16 bytes, else per cell through the cache
+    S.mat_tile = S.has_matmap && S.nx % 16 == 0;
     if (S.has_cmap) {
         S.cmap.alloc(ctx, S.ncell * 4);
         BD_CUDA(cudaMemcpy(S.cmap.p, m->c_map, S.ncell * 4, cudaMemcpyHostToDevice));

@@ -91,6 +91,7 @@ struct WvArgs {
     long long peak_start, peak_end, energy_start, energy_end, dft_start, dft_len;
     int energy_mode, n_dft, dz_lo, dz_hi;
     int relax_scheme;
+    int mat_tile;              // 1: the two-cell kernel receives the material map as a TMA tile per plane
 };
 
 // Explicitly rounded arithmetic: the compiler never re-contracts these, so

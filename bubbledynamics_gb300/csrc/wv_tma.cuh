@@ -32,6 +32,7 @@ struct TmaMaps {
     CUtensorMap rc[BD_MAX_RELAX];       // R^{n-1}
     CUtensorMap ro[BD_MAX_RELAX];       // R^{n-2}
     CUtensorMap cmap, peak, energy;
+    CUtensorMap mat;                    // box (TX, TY, 1) on the per-cell material map (uint8), when staged
 };
 
 __device__ __forceinline__ unsigned smem_u32(const void* p) {
@@ -110,8 +111,9 @@ struct TmaLayout {
     static constexpr int QT = TX * TY;
     static constexpr int QTB = QT * (int)sizeof(real);                            // bytes per real tile
     static constexpr int QTF = QT * 4;                                            // bytes of the float c tile
+    static constexpr int QTM = ((QT + 127) / 128) * 128;                          // bytes of the uint8 material tile
     static constexpr int NQR = 4 + 2 * NRMAX + 2;                                 // real tiles per slot
-    static constexpr int QS = NQR * QTB + QTF;                                    // slot bytes
+    static constexpr int QS = NQR * QTB + QTF + QTM;                              // slot bytes
     static constexpr int K_PEAK = 4 + 2 * NRMAX, K_ENERGY = 5 + 2 * NRMAX;
     static constexpr int SMEM = TMA_NP * PSLOT + NQ * QS + (TMA_NP + NQ) * 8;
 };

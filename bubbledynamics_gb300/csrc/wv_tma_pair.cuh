@@ -96,7 +96,8 @@ __global__ void __launch_bounds__(TX* TY / 2, 1536 / (TX * TY)) wv_tma_pair_kern
         const int plane = z0 + r;
         uint64_t* bar = &barQ[r % NQ];
         unsigned char* q = qslot(r);
-        mbar_expect_tx(bar, (unsigned)(((NOACC ? 4 : 6) + 2 * nrel) * L::QTB + (has_c ? L::QTF : 0)));
+        mbar_expect_tx(bar, (unsigned)(((NOACC ? 4 : 6) + 2 * nrel) * L::QTB + (has_c ? L::QTF : 0) +
+                                       (a.mat_tile ? L::QT : 0)));
         for (int k = 0; k < 4; ++k) tma_load_3d(q + k * L::QTB, &maps.q[k], bar, x0, y0, plane);
         for (int v = 0; v < nrel; ++v) {
             tma_load_3d(q + (4 + v) * L::QTB, &maps.rc[v], bar, x0, y0, plane);
@@ -107,6 +108,7 @@ __global__ void __launch_bounds__(TX* TY / 2, 1536 / (TX * TY)) wv_tma_pair_kern
             tma_load_3d(q + L::K_ENERGY * L::QTB, &maps.energy, bar, x0, y0, plane);
         }
         if (has_c) tma_load_3d(q + L::NQR * L::QTB, &maps.cmap, bar, x0, y0, plane);
+        if (a.mat_tile) tma_load_3d(q + L::NQR * L::QTB + L::QTF, &maps.mat, bar, x0, y0, plane);
     };
 
     if (tid == 0) {
@@ -215,6 +217,7 @@ __global__ void __launch_bounds__(TX* TY / 2, 1536 / (TX * TY)) wv_tma_pair_kern
         const real* pkt = reinterpret_cast<const real*>(Qs + L::K_PEAK * L::QTB);
         const real* ent = reinterpret_cast<const real*>(Qs + L::K_ENERGY * L::QTB);
         const float* ct = reinterpret_cast<const float*>(Qs + L::NQR * L::QTB);
+        const uint8_t* mtl = reinterpret_cast<const uint8_t*>(Qs + L::NQR * L::QTB + L::QTF);
         const bool src_plane = iz == a.src_iz;
         const bool zin = iz >= a.zlo && iz <= a.zhi && !src_plane;
         const bool murz = (a.mur_zp && iz >= a.nz - a.L) || (a.mur_zm && iz < a.Lzm);
@@ -311,7 +314,8 @@ __global__ void __launch_bounds__(TX* TY / 2, 1536 / (TX * TY)) wv_tma_pair_kern
                     if constexpr (FL >= 0 && (FL & 1)) {
                         pn[cx] = upd(M0);
                     } else {
-                        const int m = a.matmap ? (int)__ldg(a.matmap + zoff + col[c]) : mplane;
+                        const int m = !a.matmap ? mplane
+                                      : a.mat_tile ? (int)mtl[k + cx] : (int)__ldg(a.matmap + zoff + col[c]);
                         pn[cx] = upd(sK[m]);
                     }
                     if (a.wz) pn[cx] = mul_(pn[cx], mul_(swxy[c], wzi));
