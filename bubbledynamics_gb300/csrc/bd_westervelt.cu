@@ -85,7 +85,7 @@ struct WvSession {
     // tensor maps of the TMA variant in use (built per tile shape)
     int maps_tx = 0, maps_ty = 0;
     bool adj_fused = false;     // adjoint: one fused pass per backward step (FP32, nx % 4 == 0)
-    CUtensorMap mP0[5], mQ[5], mR[BD_MAX_RELAX][2], mC, mPeak, mEnergy, mMat;
+    CUtensorMap mP0[5], mQ[5], mR[BD_MAX_RELAX][2], mC, mPeak, mEnergy, mMat, mDre, mDim;
     bool mat_tile = false;      // the material map travels as a TMA tile (nx % 16 == 0)
     // segment view (TMA variants only): the pressure levels of the next step are
     // read from, and p^{n+1} written to, caller-chosen buffers instead of the ring
@@ -209,10 +209,10 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
 }
 
 static CUtensorMap make_map(const WvSession& S, const void* base, bool is_float, int bx, int by,
-                            bool is_u8 = false) {
+                            bool is_u8 = false, long long depth = 0) {
     CUtensorMap m;
     const size_t esz = is_u8 ? 1 : is_float ? 4 : 8;
-    cuuint64_t dims[3] = {(cuuint64_t)S.nx, (cuuint64_t)S.ny, (cuuint64_t)S.nz};
+    cuuint64_t dims[3] = {(cuuint64_t)S.nx, (cuuint64_t)S.ny, (cuuint64_t)(depth > 0 ? depth : S.nz)};
     cuuint64_t strides[2] = {(cuuint64_t)S.nx * esz, (cuuint64_t)S.nx * S.ny * esz};
     cuuint32_t box[3] = {(cuuint32_t)bx, (cuuint32_t)by, 1};
     cuuint32_t estr[3] = {1, 1, 1};
@@ -250,6 +250,11 @@ static void build_maps(WvSession& S, int tx, int ty) {
     S.mEnergy = make_map(S, S.energy.p, f, tx, ty);
     if (S.has_cmap) S.mC = make_map(S, S.cmap.p, true, tx, ty);
     if (S.mat_tile) S.mMat = make_map(S, S.matmap.p, false, tx, ty, true);
+    if (f && S.n_dft > 0) {   // the DFT planes of every frequency stacked along z (L2 prefetch only)
+        const long long depth = (long long)S.n_dft * (S.dz_hi - S.dz_lo);
+        S.mDre = make_map(S, S.dre.p, true, tx, ty, false, depth);
+        S.mDim = make_map(S, S.dim.p, true, tx, ty, false, depth);
+    }
     S.maps_tx = tx;
     S.maps_ty = ty;
 }
@@ -316,6 +321,7 @@ static void step_maps(WvSession& S, int64_t s, int tx, int ty, TmaMaps& maps) {
     maps.energy = S.mEnergy;
     if (S.has_cmap) maps.cmap = S.mC;
     if (S.mat_tile) maps.mat = S.mMat;
+    if (S.prec == BD_F32 && S.n_dft > 0) { maps.dre = S.mDre; maps.dim = S.mDim; }
 }
 
 template <class real, int TX, int TY, int CPT, int ZU>

@@ -33,6 +33,7 @@ struct TmaMaps {
     CUtensorMap ro[BD_MAX_RELAX];       // R^{n-2}
     CUtensorMap cmap, peak, energy;
     CUtensorMap mat;                    // box (TX, TY, 1) on the per-cell material map (uint8), when staged
+    CUtensorMap dre, dim;               // box (TX, TY, 1) on the DFT accumulators as (nx, ny, n_dft x planes)
 };
 
 __device__ __forceinline__ unsigned smem_u32(const void* p) {
@@ -99,6 +100,14 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, u
         "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
         ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
         : "memory");
+}
+
+// Prefetch of one tile into L2 (no shared memory, no barrier): a hint for the
+// loads that follow.
+__device__ __forceinline__ void tma_prefetch_3d(const CUtensorMap* map, int x, int y, int z) {
+    asm volatile("cp.async.bulk.prefetch.tensor.3d.L2.global.tile [%0, {%1, %2, %3}];"
+                 ::"l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z)
+                 : "memory");
 }
 
 // Shared-memory layout.  NRMAX is the number of relaxation processes the slot

@@ -91,9 +91,20 @@ __global__ void __launch_bounds__(TX* TY / 2, 1536 / (TX * TY)) wv_tma_pair_kern
         mbar_expect_tx(bar, L::PW * L::PH * (unsigned)sizeof(real));
         tma_load_3d(pslot(q), &maps.p0, bar, x0 - 4, y0 - 3, plane);
     };
+    // steps inside the DFT window: the producer also asks L2 for the plane's
+    // accumulator tiles when it issues the plane's pointwise tiles, so the
+    // accumulators' read-modify-writes find them there (set once the step is known)
+    bool pf_dft = false;
     auto issueQ = [&](int r) {
         if (r >= zbn) return;
         const int plane = z0 + r;
+        if (pf_dft && plane >= a.dz_lo && plane < a.dz_hi) {
+            const int ndz = a.dz_hi - a.dz_lo;
+            for (int j = 0; j < a.n_dft; ++j) {
+                tma_prefetch_3d(&maps.dre, x0, y0, j * ndz + plane - a.dz_lo);
+                tma_prefetch_3d(&maps.dim, x0, y0, j * ndz + plane - a.dz_lo);
+            }
+        }
         uint64_t* bar = &barQ[r % NQ];
         unsigned char* q = qslot(r);
         mbar_expect_tx(bar, (unsigned)(((NOACC ? 4 : 6) + 2 * nrel) * L::QTB + (has_c ? L::QTF : 0) +
@@ -123,6 +134,8 @@ __global__ void __launch_bounds__(TX* TY / 2, 1536 / (TX * TY)) wv_tma_pair_kern
     // read only after this wait (a no-op for an ordinary launch).
     asm volatile("griddepcontrol.wait;" ::: "memory");
     const long long step = *a.step_base + koff;
+    if constexpr (!NOACC && sizeof(real) == 4)
+        pf_dft = a.n_dft > 0 && step >= a.dft_start && step < a.dft_start + a.dft_len;
     if (tid == 0) {
         for (int q = 0; q < TMA_NP; ++q) issueP(q);
         for (int r = 0; r < NQ; ++r) issueQ(r);
