@@ -548,6 +548,8 @@ def run_adjoint(args):
     from bubbledynamics_gb300 import api, presets
     ctx = api.Context(0)
     prob, loss = presets.cfg4(n_steps=args.time_steps)
+    if args.tile_variant >= 0:
+        prob.params.tile_variant = args.tile_variant
     loss.checkpoint_every = -1
     L, gp, ga, tm = ctx.westervelt_adjoint(prob, loss)
     print(json.dumps({"workload": "cfg4 adjoint", "time_steps": args.time_steps, "timings_ms": tm}), flush=True)
@@ -604,7 +606,7 @@ def main():
     ap.add_argument("--ref-arith", action="store_true", help="gilmore workload: the reference's operation order")
     ap.add_argument("--time-steps", type=int, default=30, help="step-kernel workload: time steps per solve")
     ap.add_argument("--tile-variant", type=int, default=-1,
-                    help="step-kernel / dft workloads: tile variant (-1: every TMA variant / autotuned)")
+                    help="step-kernel / dft / adjoint workloads: tile variant (-1: every TMA variant / autotuned)")
     ap.add_argument("--cpu-sample", type=int, default=60)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extra", action="store_true", help="skip the adjoint and Gilmore summaries")
