@@ -80,8 +80,8 @@ struct WvSession {
     PoolBuf step_base, flag, kconst, Qd;
     double tau_max = 0.0;
     double last_ms = 0.0;
-    cudaGraphExec_t graph[2] = {nullptr, nullptr};   // chunk graphs: [1] for chunks that accumulate nothing
-    int graph_variant[2] = {-1, -1};
+    cudaGraphExec_t graph[3] = {nullptr, nullptr, nullptr};   // chunk graphs per accumulator mode (ACC_*)
+    int graph_variant[3] = {-1, -1, -1};
     // tensor maps of the TMA variant in use (built per tile shape)
     int maps_tx = 0, maps_ty = 0;
     bool adj_fused = false;     // adjoint: one fused pass per backward step (FP32, nx % 4 == 0)
@@ -338,22 +338,32 @@ static void launch_tma_t(WvSession& S, const WvArgs<real>& a, int64_t s, int kof
     else launch_tma_k<real, TX, TY, CPT, -1, ZU>(S, a, maps, koff, st);
 }
 
-// Whether step s adds to any accumulator (peak, energy or DFT window open).
-static bool step_accumulates(const WvSession& S, int64_t s) {
-    return (s >= S.p.peak_start && s < S.p.peak_end) || (s >= S.p.energy_start && s < S.p.energy_end) ||
-           (S.n_dft > 0 && s >= S.p.dft_start && s < S.p.dft_start + S.p.dft_len);
+// Accumulators step s adds to (the ACC_* modes of the paired kernel): all when
+// its energy or DFT window is open, the peak map only when just the peak window
+// is, none outside every window.
+static int step_acc_mode(const WvSession& S, int64_t s) {
+    if ((s >= S.p.energy_start && s < S.p.energy_end) ||
+        (S.n_dft > 0 && s >= S.p.dft_start && s < S.p.dft_start + S.p.dft_len))
+        return ACC_ALL;
+    if (s >= S.p.peak_start && s < S.p.peak_end) return ACC_PEAK;
+    return ACC_NONE;
 }
 
-static bool range_accumulates(const WvSession& S, int64_t s0, int64_t n) {
-    for (int64_t s = s0; s < s0 + n; ++s)
-        if (step_accumulates(S, s)) return true;
-    return false;
+// The mode that serves every step of [s0, s0 + n): all > peak > none.
+static int range_acc_mode(const WvSession& S, int64_t s0, int64_t n) {
+    int m = ACC_NONE;
+    for (int64_t s = s0; s < s0 + n; ++s) {
+        const int k = step_acc_mode(S, s);
+        if (k == ACC_ALL) return ACC_ALL;
+        if (k == ACC_PEAK) m = ACC_PEAK;
+    }
+    return m;
 }
 
 // Two x cells per thread (FP32; variant_ok has been checked).
 template <class real>
 static void launch_pair(WvSession& S, const WvArgs<real>& a, int64_t s, int koff, cudaStream_t st, const Variant& v,
-                        bool noacc) {
+                        int acc) {
     if constexpr (sizeof(real) != 4) {
         fail(BD_ERR_INVALID_ARG, "two-cell tile variants take FP32 fields");
     } else {
@@ -375,7 +385,7 @@ static void launch_pair(WvSession& S, const WvArgs<real>& a, int64_t s, int koff
         c.kind = S.max_relax == 0 ? 0
                  : S.max_relax == 1 ? ((S.has_cmap && !S.has_matmap && !S.has_planemat) ? 1 : 2)
                  : S.max_relax == 2 ? 3 : -1;
-        c.noacc = noacc;
+        c.acc = acc;
         wv_pair_launch(c);
     }
 }
@@ -389,14 +399,14 @@ static void launch_step_t(WvSession& S, const WvArgs<real>& a, int koff, cudaStr
 }
 
 template <class real>
-static void launch_step(WvSession& S, int variant, int64_t s, int koff, cudaStream_t st, bool noacc) {
+static void launch_step(WvSession& S, int variant, int64_t s, int koff, cudaStream_t st, int acc) {
     WvArgs<real> a = make_args<real>(S, s);
     const Variant& v = kVariants[variant];
     a.zb = v.zb > 0 ? v.zb : (v.zb < 0 && v.tma ? -1 : S.nz);
     if (v.tma && !tma_eligible(S)) fail(BD_ERR_INVALID_ARG, "tile variant %d needs a 16-byte row pitch", variant);
     if (!variant_ok(S, variant))
         fail(BD_ERR_INVALID_ARG, "tile variant %d takes FP32 fields with at most two relaxation processes", variant);
-    if (v.pair) launch_pair<real>(S, a, s, koff, st, v, noacc);
+    if (v.pair) launch_pair<real>(S, a, s, koff, st, v, acc);
     else switch (variant) {
         case 0: case 3: case 7: launch_step_t<real, 32, 8>(S, a, koff, st); break;
         case 1: launch_step_t<real, 32, 4>(S, a, koff, st); break;
@@ -434,21 +444,21 @@ static void launch_step(WvSession& S, int variant, int64_t s, int koff, cudaStre
 }
 
 // Issue steps [s, s+n) on the stream (no graph): kernels read *step_base + koff,
-// then one advance kernel moves the counter by n.  noacc < 0: each step takes
-// the accumulator-free kernel when it accumulates nothing; 0 / 1 force it
-// off / on for every step (a captured chunk).
-static void issue_steps(WvSession& S, int variant, int64_t s, int n, cudaStream_t st, int noacc = -1) {
+// then one advance kernel moves the counter by n.  acc < 0: each step takes the
+// paired kernel that touches only the accumulators it needs (step_acc_mode);
+// an ACC_* mode forces that one for every step (a captured chunk).
+static void issue_steps(WvSession& S, int variant, int64_t s, int n, cudaStream_t st, int acc = -1) {
     for (int k = 0; k < n; ++k) {
-        const bool na = noacc >= 0 ? noacc != 0 : !step_accumulates(S, s + k);
-        if (S.prec == BD_F32) launch_step<float>(S, variant, s + k, k, st, na);
-        else launch_step<double>(S, variant, s + k, k, st, na);
+        const int m = acc >= 0 ? acc : step_acc_mode(S, s + k);
+        if (S.prec == BD_F32) launch_step<float>(S, variant, s + k, k, st, m);
+        else launch_step<double>(S, variant, s + k, k, st, m);
     }
     wv_advance_kernel<<<1, 32, 0, st>>>(S.step_base.as<long long>(), n);
     BD_LAUNCHED(S.ctx);
 }
 
-static void build_graph(WvSession& S, int noacc) {
-    cudaGraphExec_t& G = S.graph[noacc];
+static void build_graph(WvSession& S, int acc) {
+    cudaGraphExec_t& G = S.graph[acc];
     if (G) { cudaGraphExecDestroy(G); G = nullptr; }
     cudaStream_t cs;
     BD_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
@@ -456,7 +466,7 @@ static void build_graph(WvSession& S, int noacc) {
     const int64_t launches_before = S.ctx->launches;
     BD_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
     try {
-        issue_steps(S, S.variant, 0, S.chunk, cs, noacc);   // base arrangement: chunk starts at s = 0 mod 10
+        issue_steps(S, S.variant, 0, S.chunk, cs, acc);   // base arrangement: chunk starts at s = 0 mod 10
     } catch (...) {
         cudaStreamEndCapture(cs, &g);
         if (g) cudaGraphDestroy(g);
@@ -469,7 +479,7 @@ static void build_graph(WvSession& S, int noacc) {
     cudaGraphDestroy(g);
     cudaStreamDestroy(cs);
     BD_CUDA(e);
-    S.graph_variant[noacc] = S.variant;
+    S.graph_variant[acc] = S.variant;
 }
 
 static int64_t launches_per_step(const WvSession& S) {
@@ -512,9 +522,9 @@ static void advance(WvSession& S, int64_t n, bool use_graph) {
         const int64_t to_align = (S.chunk - (S.step % S.chunk)) % S.chunk;
         int64_t take;
         if (use_graph && to_align == 0 && todo >= S.chunk) {
-            const int na = range_accumulates(S, S.step, S.chunk) ? 0 : 1;
-            if (!S.graph[na] || S.graph_variant[na] != S.variant) build_graph(S, na);
-            BD_CUDA(cudaGraphLaunch(S.graph[na], st));
+            const int m = range_acc_mode(S, S.step, S.chunk);
+            if (!S.graph[m] || S.graph_variant[m] != S.variant) build_graph(S, m);
+            BD_CUDA(cudaGraphLaunch(S.graph[m], st));
             S.ctx->launches += per * S.chunk + 1;
             take = S.chunk;
         } else {

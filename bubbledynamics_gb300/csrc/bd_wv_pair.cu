@@ -9,10 +9,10 @@
 
 namespace bd {
 
-template <int TX, int TY, int NREL, int ZU, int FL, int NQ, bool NOACC>
+template <int TX, int TY, int NREL, int ZU, int FL, int NQ, int ACC>
 static void pair_k(const PairCall& c) {
     using L = TmaLayout<float, TX, TY, (NREL >= 0 ? NREL : BD_MAX_RELAX), NQ>;
-    auto kern = wv_tma_pair_kernel<float, TX, TY, NREL, ZU, FL, NQ, NOACC>;
+    auto kern = wv_tma_pair_kernel<float, TX, TY, NREL, ZU, FL, NQ, ACC>;
     static bool attr_done = false;
     static int per_sm = 0;
     if (!attr_done) {
@@ -50,22 +50,25 @@ static void pair_k(const PairCall& c) {
 
 // material layout: 0 = no relaxation, 1 = one process, one material and a c
 // map (compile-time), 2 = one process, 3 = two processes
-template <int TX, int TY, int ZU, int NQ, bool NOACC>
+template <int TX, int TY, int ZU, int NQ, int ACC>
 static void pair_kind_acc(const PairCall& c) {
     switch (c.kind) {
-        case 0: pair_k<TX, TY, 0, ZU, -1, NQ, NOACC>(c); break;
-        case 1: pair_k<TX, TY, 1, ZU, 3, NQ, NOACC>(c); break;
-        case 2: pair_k<TX, TY, 1, ZU, -1, NQ, NOACC>(c); break;
-        case 3: pair_k<TX, TY, 2, ZU, -1, NQ, NOACC>(c); break;
+        case 0: pair_k<TX, TY, 0, ZU, -1, NQ, ACC>(c); break;
+        case 1: pair_k<TX, TY, 1, ZU, 3, NQ, ACC>(c); break;
+        case 2: pair_k<TX, TY, 1, ZU, -1, NQ, ACC>(c); break;
+        case 3: pair_k<TX, TY, 2, ZU, -1, NQ, ACC>(c); break;
         default: fail(BD_ERR_INVALID_ARG, "two-cell tile variants take at most two relaxation processes");
     }
 }
 
-// steps without accumulation take the kernel that leaves the accumulators alone
+// steps outside some accumulator windows take the kernel that skips those accumulators
 template <int TX, int TY, int ZU, int NQ>
 static void pair_kind(const PairCall& c) {
-    if (c.noacc) pair_kind_acc<TX, TY, ZU, NQ, true>(c);
-    else pair_kind_acc<TX, TY, ZU, NQ, false>(c);
+    switch (c.acc) {
+        case ACC_NONE: pair_kind_acc<TX, TY, ZU, NQ, ACC_NONE>(c); break;
+        case ACC_PEAK: pair_kind_acc<TX, TY, ZU, NQ, ACC_PEAK>(c); break;
+        default: pair_kind_acc<TX, TY, ZU, NQ, ACC_ALL>(c); break;
+    }
 }
 
 void wv_pair_launch(const PairCall& c) {

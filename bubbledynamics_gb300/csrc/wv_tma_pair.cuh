@@ -40,10 +40,12 @@ __device__ __forceinline__ void st2(real* p, real v0, real v1) {
 // for 24 resident warps per SM (at most 85 registers a thread).  The cell update is
 // cell_update(), so the results are the plain kernel's bits.
 //
-// NOACC: a step without any accumulation (outside the peak, energy and DFT
-// windows, e.g. the recompute of the adjoint) neither loads the peak / energy
-// tiles nor touches the accumulators: 8 B less per cell.
-template <class real, int TX, int TY, int NREL, int ZU, int FL, int NQ, bool NOACC = false>
+// ACC: which accumulators the step may touch.  ACC_ALL: peak, energy and DFT
+// (each still gated by its window); ACC_PEAK: only the peak map (a step outside
+// the energy and DFT windows: the energy tile is not loaded, 4 B less per
+// cell); ACC_NONE: none (outside every window, e.g. the recompute of the
+// adjoint: neither tile is loaded, 8 B less per cell).
+template <class real, int TX, int TY, int NREL, int ZU, int FL, int NQ, int ACC = ACC_ALL>
 __global__ void __launch_bounds__(TX* TY / 2, 1536 / (TX * TY)) wv_tma_pair_kernel(const WvArgs<real> a,
                                                                  const WvConst<real>* __restrict__ Kp, int koff,
                                                                  const __grid_constant__ TmaMaps maps,
@@ -107,17 +109,16 @@ __global__ void __launch_bounds__(TX* TY / 2, 1536 / (TX * TY)) wv_tma_pair_kern
         }
         uint64_t* bar = &barQ[r % NQ];
         unsigned char* q = qslot(r);
-        mbar_expect_tx(bar, (unsigned)(((NOACC ? 4 : 6) + 2 * nrel) * L::QTB + (has_c ? L::QTF : 0) +
+        constexpr int acc_tiles = ACC == ACC_ALL ? 2 : ACC == ACC_PEAK ? 1 : 0;
+        mbar_expect_tx(bar, (unsigned)((4 + acc_tiles + 2 * nrel) * L::QTB + (has_c ? L::QTF : 0) +
                                        (a.mat_tile ? L::QT : 0)));
         for (int k = 0; k < 4; ++k) tma_load_3d(q + k * L::QTB, &maps.q[k], bar, x0, y0, plane);
         for (int v = 0; v < nrel; ++v) {
             tma_load_3d(q + (4 + v) * L::QTB, &maps.rc[v], bar, x0, y0, plane);
             tma_load_3d(q + (4 + NRMAX + v) * L::QTB, &maps.ro[v], bar, x0, y0, plane);
         }
-        if constexpr (!NOACC) {
-            tma_load_3d(q + L::K_PEAK * L::QTB, &maps.peak, bar, x0, y0, plane);
-            tma_load_3d(q + L::K_ENERGY * L::QTB, &maps.energy, bar, x0, y0, plane);
-        }
+        if constexpr (ACC != ACC_NONE) tma_load_3d(q + L::K_PEAK * L::QTB, &maps.peak, bar, x0, y0, plane);
+        if constexpr (ACC == ACC_ALL) tma_load_3d(q + L::K_ENERGY * L::QTB, &maps.energy, bar, x0, y0, plane);
         if (has_c) tma_load_3d(q + L::NQR * L::QTB, &maps.cmap, bar, x0, y0, plane);
         if (a.mat_tile) tma_load_3d(q + L::NQR * L::QTB + L::QTF, &maps.mat, bar, x0, y0, plane);
     };
@@ -134,7 +135,7 @@ __global__ void __launch_bounds__(TX* TY / 2, 1536 / (TX * TY)) wv_tma_pair_kern
     // read only after this wait (a no-op for an ordinary launch).
     asm volatile("griddepcontrol.wait;" ::: "memory");
     const long long step = *a.step_base + koff;
-    if constexpr (!NOACC && sizeof(real) == 4)
+    if constexpr (ACC == ACC_ALL && sizeof(real) == 4)
         pf_dft = a.n_dft > 0 && step >= a.dft_start && step < a.dft_start + a.dft_len;
     if (tid == 0) {
         for (int q = 0; q < TMA_NP; ++q) issueP(q);
@@ -184,10 +185,10 @@ __global__ void __launch_bounds__(TX* TY / 2, 1536 / (TX * TY)) wv_tma_pair_kern
         for (int q = TMA_NP; q < TMA_NP + 3; ++q) issueP(q);
 
     const bool fix_x = a.mir_x && x0 == 0, fix_y = a.mir_y && y0 == 0;
-    const bool do_peak = !NOACC && step >= a.peak_start && step < a.peak_end;
-    const bool do_energy = !NOACC && step >= a.energy_start && step < a.energy_end;
+    const bool do_peak = ACC != ACC_NONE && step >= a.peak_start && step < a.peak_end;
+    const bool do_energy = ACC == ACC_ALL && step >= a.energy_start && step < a.energy_end;
     const long long ds = step - a.dft_start;
-    const bool do_dft = !NOACC && a.n_dft > 0 && ds >= 0 && ds < a.dft_len;
+    const bool do_dft = ACC == ACC_ALL && a.n_dft > 0 && ds >= 0 && ds < a.dft_len;
     const bool single_mat = FL >= 0 ? (FL & 1) != 0 : (!a.matmap && !a.plane_mat);
     const bool dpdt = a.energy_mode == BD_ENERGY_DPDT2;
     // the material of single-material problems, in registers

@@ -328,9 +328,10 @@ def test_cfg1_full_size_f32_accuracy(ctx, cfg1_full_oracle):
 @pytest.mark.parametrize("chunk", [20, -1])
 def test_partial_windows_take_the_accumulator_free_kernel(ctx, chunk):
     """Peak and energy windows that cover only part of the run: steps outside
-    both windows run the paired kernel without accumulators (whole captured
-    chunks or single steps), and every output equals the one-cell kernel's,
-    which always carries the accumulators."""
+    both windows run the paired kernel without accumulators, steps inside the
+    peak window only run its peak-only mode (whole captured chunks or single
+    steps), and every output equals the one-cell kernel's, which always
+    carries the accumulators."""
     res = {}
     for v in (21, 17):
         p = presets.cfg1(40, 40, 64, 230, precision=abi.BD_F32)
