@@ -1,6 +1,8 @@
 // Two-cells-per-thread variant of the TMA-pipelined Westervelt step (sm_103a).
 #pragma once
 
+#include <type_traits>
+
 #include "wv_tma.cuh"
 
 namespace bd {
@@ -180,7 +182,13 @@ __global__ void __launch_bounds__(TX* TY / 2, 1536 / (TX * TY)) wv_tma_pair_kern
         const int plane = z0 - 3 + k;
         load_w(pslot(k), plane >= 0 && plane < a.nz, k);
     }
-    __syncthreads();                               // slots of planes z0-3..z0-1 are free again
+    // every cell of the tile inside the grid and the update box and on no x / y
+    // Mur layer: the planes of the tile inside the z range take the code without
+    // per-cell conditions (the same operations on every cell, so the same bits)
+    bool mine = true;
+#pragma unroll
+    for (int c = 0; c < NC; ++c) mine = mine && active[c] && inbox[c] && !murxy[c];
+    const bool tile_fast = __syncthreads_and(mine) != 0;   // also: slots of planes z0-3..z0-1 are free again
     if (tid == 0)
         for (int q = TMA_NP; q < TMA_NP + 3; ++q) issueP(q);
 
@@ -244,10 +252,13 @@ __global__ void __launch_bounds__(TX* TY / 2, 1536 / (TX * TY)) wv_tma_pair_kern
         real* rolz[NRMAX > 0 ? NRMAX : 1];
 #pragma unroll
         for (int v = 0; v < NRMAX; ++v) rolz[v] = a.rold[v] + zoff;
+        // FAST: every cell of the tile is updated and accumulates on this plane
+        auto cells = [&](auto fast_tag) {
+        constexpr bool FAST = decltype(fast_tag)::value;
 #pragma unroll
         for (int cy = 0; cy < CPT; ++cy) {
             const int c0 = cy * CX;                // first cell of this row (the CX cells share `active`)
-            if (!active[c0]) continue;
+            if (!FAST && !active[c0]) continue;
             const int k = qi[c0];
             real q1[CX], pn[CX];
             bool have[CX];
@@ -256,13 +267,13 @@ __global__ void __launch_bounds__(TX* TY / 2, 1536 / (TX * TY)) wv_tma_pair_kern
             ldx<CX>(q1t + k, q1);
 #pragma unroll
             for (int cx = 0; cx < CX; ++cx) { have[cx] = false; nrx[cx] = 0; }
-            if (src_plane) {
+            if (!FAST && src_plane) {
 #pragma unroll
                 for (int cx = 0; cx < CX; ++cx) {
                     pn[cx] = source_value<real>(a, step, (int)col[c0 + cx]);
                     have[cx] = true;
                 }
-            } else if (zin) {
+            } else if (FAST || zin) {
                 // x and y neighbours of the CX cells from the plane tile
                 const real* cp = T + own[c0];
                 constexpr int W = L::PW;
@@ -317,7 +328,7 @@ __global__ void __launch_bounds__(TX* TY / 2, 1536 / (TX * TY)) wv_tma_pair_kern
 #pragma unroll
                 for (int cx = 0; cx < CX; ++cx) {
                     const int c = c0 + cx;
-                    if (!inbox[c]) continue;
+                    if (!FAST && !inbox[c]) continue;
                     auto upd = [&](const MatConst<real>& M) -> real {
                         const real r = cell_update<real, NRMAX>(a, M, has_c ? cs[cx] : M.c0, w[c][3], sx1[cx], sx2[cx],
                                                                 sx3[cx], sy1[cx], sy2[cx], sy3[cx], w[c], q1[cx],
@@ -337,7 +348,7 @@ __global__ void __launch_bounds__(TX* TY / 2, 1536 / (TX * TY)) wv_tma_pair_kern
                 }
             }
             // stores: a pair access where both cells take part, else per cell
-            const bool pair = CX == 2 && have[0] && have[CX - 1];
+            const bool pair = CX == 2 && (FAST || (have[0] && have[CX - 1]));
             if (pair) st2(p4z + col[c0], pn[0], pn[CX - 1]);
             else
 #pragma unroll
@@ -354,7 +365,7 @@ __global__ void __launch_bounds__(TX* TY / 2, 1536 / (TX * TY)) wv_tma_pair_kern
             }
             bool acc[CX];
 #pragma unroll
-            for (int cx = 0; cx < CX; ++cx) acc[cx] = have[cx] && !(murz || murxy[c0 + cx]);
+            for (int cx = 0; cx < CX; ++cx) acc[cx] = FAST || (have[cx] && !(murz || murxy[c0 + cx]));
             const bool acc_pair = CX == 2 && acc[0] && acc[CX - 1];
             if (do_peak) {
                 real pk[CX], pv[CX];
@@ -448,6 +459,9 @@ __global__ void __launch_bounds__(TX* TY / 2, 1536 / (TX * TY)) wv_tma_pair_kern
                 }
             }
         }
+        };
+        if (tile_fast && zin && !murz) cells(std::true_type{});
+        else cells(std::false_type{});
 #pragma unroll
         for (int c = 0; c < NC; ++c)
 #pragma unroll
