@@ -138,10 +138,12 @@ def dist_barrier(world):
         dist.barrier()
 
 
-def cfg1_problem(precision=None):
+def cfg1_problem(precision=None, tile_variant=-1):
     from bubbledynamics_gb300 import abi, presets
-    return presets.cfg1(CFG1["nx"], CFG1["ny"], CFG1["nz"], CFG1["n_steps"],
-                        precision=abi.BD_F32 if precision is None else precision)
+    p = presets.cfg1(CFG1["nx"], CFG1["ny"], CFG1["nz"], CFG1["n_steps"],
+                     precision=abi.BD_F32 if precision is None else precision)
+    p.params.tile_variant = tile_variant
+    return p
 
 
 def cpu_baseline_port(sample_steps):
@@ -223,7 +225,8 @@ def run_westervelt(args, world, rank, local):
     ncell = CFG1["nx"] * CFG1["ny"] * CFG1["nz"]
     T = CFG1["n_steps"]
     # ---- device-resident solves (value)
-    sessions = [ctx.westervelt_session(cfg1_problem()) for _ in range(args.warmup + args.steps)]
+    sessions = [ctx.westervelt_session(cfg1_problem(tile_variant=args.tile_variant))
+                for _ in range(args.warmup + args.steps)]
     for s in sessions[: args.warmup]:
         s.advance(T)
     dist_barrier(world)
@@ -251,7 +254,7 @@ def run_westervelt(args, world, rank, local):
             "frac": achieved / pk["hbm_gbs"], "traffic": NCU_TRAFFIC_BYTES,
             "algorithmic_bytes": BYTES_PER_CELL * ncell, "peak_kind": pk_kind}
     # ---- end to end through the C ABI with host buffers
-    prob = cfg1_problem()
+    prob = cfg1_problem(tile_variant=args.tile_variant)
     cmap = prob.array("c_map")
     h2d = cmap.nbytes + prob.grid.nx * prob.grid.ny * (4 + 4 * 4 + 4) + T * (8 + 16 + 4)
     d2h = 2 * ncell * 4
@@ -606,7 +609,7 @@ def main():
     ap.add_argument("--ref-arith", action="store_true", help="gilmore workload: the reference's operation order")
     ap.add_argument("--time-steps", type=int, default=30, help="step-kernel workload: time steps per solve")
     ap.add_argument("--tile-variant", type=int, default=-1,
-                    help="step-kernel / dft / adjoint workloads: tile variant (-1: every TMA variant / autotuned)")
+                    help="tile variant (-1: autotuned; the step-kernel workload then times every TMA variant)")
     ap.add_argument("--cpu-sample", type=int, default=60)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extra", action="store_true", help="skip the adjoint and Gilmore summaries")

@@ -40,3 +40,19 @@ def test_cfg5_bubbles_driven_by_local_field(ctx, oracle):
     ro = oracle.gilmore(med, (abi.Bubble * len(b)).from_buffer_copy(b.tobytes()), ode)
     assert np.all(res["status"] == abi.BD_BUBBLE_DONE)
     np.testing.assert_allclose(res["R"], [x.R for x in ro], rtol=1e-6)
+
+
+def test_cfg5_dft_same_bits_in_every_tile_variant(ctx):
+    """The DFT accumulators through the one-cell kernel and the two-cell
+    kernels (pair read-modify-writes of the accumulator planes), with two
+    relaxation processes and three tones: the same bits."""
+    res = {}
+    for v in (17, 21, 23):
+        p = _small()
+        p.params.tile_variant = v
+        res[v] = ctx.westervelt(p, want=("p_final", "peak", "energy", "dft"))
+        assert res[v]["tile_variant"] == v
+    assert np.abs(res[17]["dft_re"]).max() > 0
+    for v in (21, 23):
+        for k in ("p_final", "peak", "energy", "dft_re", "dft_im"):
+            np.testing.assert_array_equal(res[v][k], res[17][k], err_msg="variant %d, %s" % (v, k))
