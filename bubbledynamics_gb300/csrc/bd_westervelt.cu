@@ -80,8 +80,8 @@ struct WvSession {
     PoolBuf step_base, flag, kconst, Qd;
     double tau_max = 0.0;
     double last_ms = 0.0;
-    cudaGraphExec_t graph[3] = {nullptr, nullptr, nullptr};   // chunk graphs per accumulator mode (ACC_*)
-    int graph_variant[3] = {-1, -1, -1};
+    cudaGraphExec_t graph[4] = {nullptr, nullptr, nullptr, nullptr};   // chunk graphs per accumulator mode (ACC_*)
+    int graph_variant[4] = {-1, -1, -1, -1};
     // tensor maps of the TMA variant in use (built per tile shape)
     int maps_tx = 0, maps_ty = 0;
     bool adj_fused = false;     // adjoint: one fused pass per backward step (FP32, nx % 4 == 0)
@@ -339,23 +339,23 @@ static void launch_tma_t(WvSession& S, const WvArgs<real>& a, int64_t s, int kof
 }
 
 // Accumulators step s adds to (the ACC_* modes of the paired kernel): all when
-// its energy or DFT window is open, the peak map only when just the peak window
-// is, none outside every window.
+// its DFT window is open, peak and energy when the energy window is, the peak
+// map only when just the peak window is, none outside every window.
 static int step_acc_mode(const WvSession& S, int64_t s) {
-    if ((s >= S.p.energy_start && s < S.p.energy_end) ||
-        (S.n_dft > 0 && s >= S.p.dft_start && s < S.p.dft_start + S.p.dft_len))
-        return ACC_ALL;
+    if (S.n_dft > 0 && s >= S.p.dft_start && s < S.p.dft_start + S.p.dft_len) return ACC_ALL;
+    if (s >= S.p.energy_start && s < S.p.energy_end) return ACC_PE;
     if (s >= S.p.peak_start && s < S.p.peak_end) return ACC_PEAK;
     return ACC_NONE;
 }
 
-// The mode that serves every step of [s0, s0 + n): all > peak > none.
+// The mode that serves every step of [s0, s0 + n): all > peak and energy > peak > none.
 static int range_acc_mode(const WvSession& S, int64_t s0, int64_t n) {
+    auto rank = [](int m) { return m == ACC_ALL ? 3 : m == ACC_PE ? 2 : m == ACC_PEAK ? 1 : 0; };
     int m = ACC_NONE;
     for (int64_t s = s0; s < s0 + n; ++s) {
         const int k = step_acc_mode(S, s);
-        if (k == ACC_ALL) return ACC_ALL;
-        if (k == ACC_PEAK) m = ACC_PEAK;
+        if (rank(k) > rank(m)) m = k;
+        if (m == ACC_ALL) break;
     }
     return m;
 }

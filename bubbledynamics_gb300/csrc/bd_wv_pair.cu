@@ -67,6 +67,7 @@ static void pair_kind(const PairCall& c) {
     switch (c.acc) {
         case ACC_NONE: pair_kind_acc<TX, TY, ZU, NQ, ACC_NONE>(c); break;
         case ACC_PEAK: pair_kind_acc<TX, TY, ZU, NQ, ACC_PEAK>(c); break;
+        case ACC_PE: pair_kind_acc<TX, TY, ZU, NQ, ACC_PE>(c); break;
         default: pair_kind_acc<TX, TY, ZU, NQ, ACC_ALL>(c); break;
     }
 }

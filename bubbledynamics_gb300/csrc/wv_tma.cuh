@@ -24,8 +24,9 @@
 namespace bd {
 
 constexpr int TMA_NP = 8;   // p^n plane slots (>= 7)
-// accumulator modes of the paired step kernel: all windows, none, the peak map only
-constexpr int ACC_ALL = 0, ACC_NONE = 1, ACC_PEAK = 2;
+// accumulator modes of the paired step kernel: all (peak, energy and the DFT),
+// none, the peak map only, peak and energy without the DFT
+constexpr int ACC_ALL = 0, ACC_NONE = 1, ACC_PEAK = 2, ACC_PE = 3;
 constexpr int TMA_NQ = 3;   // pointwise slots
 
 struct TmaMaps {

@@ -43,10 +43,14 @@ __device__ __forceinline__ void st2(real* p, real v0, real v1) {
 // cell_update(), so the results are the plain kernel's bits.
 //
 // ACC: which accumulators the step may touch.  ACC_ALL: peak, energy and DFT
-// (each still gated by its window); ACC_PEAK: only the peak map (a step outside
-// the energy and DFT windows: the energy tile is not loaded, 4 B less per
-// cell); ACC_NONE: none (outside every window, e.g. the recompute of the
-// adjoint: neither tile is loaded, 8 B less per cell).
+// (each still gated by its window); ACC_PE: peak and energy (a step outside the
+// DFT window: no DFT code, so fewer registers); ACC_PEAK: only the peak map (a
+// step outside the energy and DFT windows: the energy tile is not loaded, 4 B
+// less per cell); ACC_NONE: none (outside every window, e.g. the recompute of
+// the adjoint: neither tile is loaded, 8 B less per cell).  Planes on which
+// every cell of the tile is updated take a copy of the cell code without the
+// per-cell conditions, except in ACC_ALL, where the larger DFT code of that
+// copy would cost registers (and spills) in the whole kernel.
 template <class real, int TX, int TY, int NREL, int ZU, int FL, int NQ, int ACC = ACC_ALL>
 __global__ void __launch_bounds__(TX* TY / 2, 1536 / (TX * TY)) wv_tma_pair_kernel(const WvArgs<real> a,
                                                                  const WvConst<real>* __restrict__ Kp, int koff,
@@ -111,7 +115,7 @@ __global__ void __launch_bounds__(TX* TY / 2, 1536 / (TX * TY)) wv_tma_pair_kern
         }
         uint64_t* bar = &barQ[r % NQ];
         unsigned char* q = qslot(r);
-        constexpr int acc_tiles = ACC == ACC_ALL ? 2 : ACC == ACC_PEAK ? 1 : 0;
+        constexpr int acc_tiles = ACC == ACC_ALL || ACC == ACC_PE ? 2 : ACC == ACC_PEAK ? 1 : 0;
         mbar_expect_tx(bar, (unsigned)((4 + acc_tiles + 2 * nrel) * L::QTB + (has_c ? L::QTF : 0) +
                                        (a.mat_tile ? L::QT : 0)));
         for (int k = 0; k < 4; ++k) tma_load_3d(q + k * L::QTB, &maps.q[k], bar, x0, y0, plane);
@@ -120,7 +124,8 @@ __global__ void __launch_bounds__(TX* TY / 2, 1536 / (TX * TY)) wv_tma_pair_kern
             tma_load_3d(q + (4 + NRMAX + v) * L::QTB, &maps.ro[v], bar, x0, y0, plane);
         }
         if constexpr (ACC != ACC_NONE) tma_load_3d(q + L::K_PEAK * L::QTB, &maps.peak, bar, x0, y0, plane);
-        if constexpr (ACC == ACC_ALL) tma_load_3d(q + L::K_ENERGY * L::QTB, &maps.energy, bar, x0, y0, plane);
+        if constexpr (ACC == ACC_ALL || ACC == ACC_PE)
+            tma_load_3d(q + L::K_ENERGY * L::QTB, &maps.energy, bar, x0, y0, plane);
         if (has_c) tma_load_3d(q + L::NQR * L::QTB, &maps.cmap, bar, x0, y0, plane);
         if (a.mat_tile) tma_load_3d(q + L::NQR * L::QTB + L::QTF, &maps.mat, bar, x0, y0, plane);
     };
@@ -185,16 +190,21 @@ __global__ void __launch_bounds__(TX* TY / 2, 1536 / (TX * TY)) wv_tma_pair_kern
     // every cell of the tile inside the grid and the update box and on no x / y
     // Mur layer: the planes of the tile inside the z range take the code without
     // per-cell conditions (the same operations on every cell, so the same bits)
-    bool mine = true;
+    bool tile_fast = false;
+    if constexpr (ACC != ACC_ALL) {
+        bool mine = true;
 #pragma unroll
-    for (int c = 0; c < NC; ++c) mine = mine && active[c] && inbox[c] && !murxy[c];
-    const bool tile_fast = __syncthreads_and(mine) != 0;   // also: slots of planes z0-3..z0-1 are free again
+        for (int c = 0; c < NC; ++c) mine = mine && active[c] && inbox[c] && !murxy[c];
+        tile_fast = __syncthreads_and(mine) != 0;      // also: slots of planes z0-3..z0-1 are free again
+    } else {
+        __syncthreads();                               // slots of planes z0-3..z0-1 are free again
+    }
     if (tid == 0)
         for (int q = TMA_NP; q < TMA_NP + 3; ++q) issueP(q);
 
     const bool fix_x = a.mir_x && x0 == 0, fix_y = a.mir_y && y0 == 0;
     const bool do_peak = ACC != ACC_NONE && step >= a.peak_start && step < a.peak_end;
-    const bool do_energy = ACC == ACC_ALL && step >= a.energy_start && step < a.energy_end;
+    const bool do_energy = (ACC == ACC_ALL || ACC == ACC_PE) && step >= a.energy_start && step < a.energy_end;
     const long long ds = step - a.dft_start;
     const bool do_dft = ACC == ACC_ALL && a.n_dft > 0 && ds >= 0 && ds < a.dft_len;
     const bool single_mat = FL >= 0 ? (FL & 1) != 0 : (!a.matmap && !a.plane_mat);
@@ -460,8 +470,12 @@ __global__ void __launch_bounds__(TX* TY / 2, 1536 / (TX * TY)) wv_tma_pair_kern
             }
         }
         };
-        if (tile_fast && zin && !murz) cells(std::true_type{});
-        else cells(std::false_type{});
+        if constexpr (ACC != ACC_ALL) {
+            if (tile_fast && zin && !murz) cells(std::true_type{});
+            else cells(std::false_type{});
+        } else {
+            cells(std::false_type{});
+        }
 #pragma unroll
         for (int c = 0; c < NC; ++c)
 #pragma unroll

@@ -16,7 +16,8 @@ struct PairCall {
     cudaStream_t st;
     int tx, ty, zu, nq;                 // tile, planes per barrier, pointwise ring slots
     int kind;                           // 0: no relaxation, 1: one process + one material + c map, 2: one, 3: two
-    int acc;                            // accumulators the step may touch: 0 all, 1 none, 2 the peak map only
+    int acc;                            // accumulators the step may touch (ACC_*): 0 all, 1 none, 2 the peak
+                                        // map only, 3 peak and energy
 };
 
 void wv_pair_launch(const PairCall& c);
