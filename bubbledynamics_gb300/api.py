@@ -74,6 +74,7 @@ def load(path=None):
     _sig(L, "bd_trajectory_shifts", [P, P, P, C.c_int64, C.POINTER(C.c_int64), P, C.c_int32])
     _sig(L, "bd_unfold_quarter", [P, C.c_int32, C.c_int32, P])
     _sig(L, "bd_spiral_heat_run", [P, P, P, P, C.c_int64, P])
+    _sig(L, "bd_spiral_heat_run_slabs", [P, P, P, P, C.c_int64, C.c_int32, P])
     _sig(L, "bd_gilmore_combo_tones", [C.c_double, P, P, P])
     _sig(L, "bd_gilmore_combos", [C.c_int32, C.c_double, C.c_double, P, C.c_int64, C.POINTER(C.c_int64)])
     _sig(L, "bd_gilmore_run", [P, P, C.c_int64, P, P, P, C.POINTER(C.c_double)])
@@ -288,7 +289,10 @@ class Context:
         return L.value, gp, ga, {"forward_ms": tm[0], "recompute_ms": tm[1], "backward_ms": tm[2]}
 
     # ------------------------------------------------------------ heat
-    def heat(self, thermal, Q, traj, max_steps=0, snapshot_legs=(), want_T=True, want_dose=True):
+    def heat(self, thermal, Q, traj, max_steps=0, snapshot_legs=(), want_T=True, want_dose=True, n_slabs=1):
+        """Heat + dose run over the trajectory (bd_spiral_heat_run); n_slabs > 1
+        runs it as that many z slabs with ghost-plane exchange
+        (bd_spiral_heat_run_slabs), which gives the same bits."""
         n = thermal.nx * thermal.ny * thermal.nz
         Q = np.ascontiguousarray(Q, dtype=np.float64).reshape(-1)
         assert Q.size == n
@@ -306,7 +310,12 @@ class Context:
             out.snapshots = _ptr(res["snapshots"])
             out.snapshot_legs = _ptr(legs)
             out.n_snap = legs.size
-        check(self.L.bd_spiral_heat_run(self.h, C.byref(thermal), _ptr(Q), C.byref(traj), max_steps, C.byref(out)))
+        if n_slabs == 1:
+            check(self.L.bd_spiral_heat_run(self.h, C.byref(thermal), _ptr(Q), C.byref(traj), max_steps,
+                                            C.byref(out)))
+        else:
+            check(self.L.bd_spiral_heat_run_slabs(self.h, C.byref(thermal), _ptr(Q), C.byref(traj), max_steps,
+                                                  int(n_slabs), C.byref(out)))
         shp = (thermal.nz, thermal.ny, thermal.nx)
         for k in ("T", "dose"):
             if k in res:

@@ -541,6 +541,12 @@ class ThermalProblem:
         self._keep["plane_material"] = pm
         self.thermal.plane_material = abi.ptr(pm)
 
+    def set_material_map(self, m):
+        """Per-cell material indices (uint8, nz x ny x nx); overrides the plane materials."""
+        m = np.ascontiguousarray(m, dtype=np.uint8)
+        self._keep["material_map"] = m
+        self.thermal.material_map = abi.ptr(m)
+
     def set_spots(self, sx, sy, steps):
         sx = np.ascontiguousarray(sx, dtype=np.int32)
         sy = np.ascontiguousarray(sy, dtype=np.int32)

@@ -384,6 +384,15 @@ typedef struct bd_heat_outputs {
 bd_status bd_spiral_heat_run(bd_context* ctx, const bd_thermal* thermal, const double* Q,
                              const bd_trajectory* traj, int64_t max_steps,
                              bd_heat_outputs* out);
+/* The same run as n_slabs z slabs on this context's device (the z-slab split
+ * of a multi-GPU heat solve, each slab its own buffers): slab k owns planes
+ * [nz k / n_slabs, nz (k + 1) / n_slabs) and keeps one ghost plane beyond each
+ * internal face (the stencil reads iz +- 1, T:72-73), refreshed from the
+ * neighbour after every step.  Outputs as bd_spiral_heat_run (the whole grid),
+ * equal to its bit for bit; 1 <= n_slabs <= nz / 2. */
+bd_status bd_spiral_heat_run_slabs(bd_context* ctx, const bd_thermal* thermal, const double* Q,
+                                   const bd_trajectory* traj, int64_t max_steps, int32_t n_slabs,
+                                   bd_heat_outputs* out);
 
 /* Allocation-free variant of the FP32 heat + dose run, for callers that
  * cannot call cudaMalloc: code running inside another framework's memory

@@ -94,3 +94,38 @@ def test_heat_graph_and_plain_launches_identical(ctx, precision):
         res.append(r)
     for key in ("T", "dose", "snapshots"):
         np.testing.assert_array_equal(res[0][key], res[1][key], err_msg=key)
+
+
+@pytest.mark.parametrize("precision,nxy,plain", [(abi.BD_F32, 44, 0), (abi.BD_F32, 41, 1), (abi.BD_F64, 41, 0)])
+def test_heat_slabs_equal_single_domain(ctx, precision, nxy, plain):
+    """The z-slab split of the heat run: 2, 3 and 7 slabs, each with its own
+    buffers and one ghost plane per internal face refreshed after every step,
+    give the one-domain temperature, dose and snapshots bit for bit.  Covers
+    the four-cell FP32 kernel (nx % 4 == 0), the scalar FP32 and FP64 kernels,
+    graphs and plain launches, snapshots at odd steps, the water/tissue plane
+    materials and a per-cell material map."""
+    k = presets.ref_T_mini_constants(Nxy=nxy, Nz=40, legs=2)
+    Q = presets.gaussian_focus_Q((40, nxy, nxy), (22, 20, 20), (3.0, 2.0, 2.0), 4.0e7)
+    rng = np.random.default_rng(5)
+    mm = (rng.random((40, nxy, nxy)) < 0.5).astype(np.uint8)
+    for with_map in (False, True):
+        res = {}
+        for n_slabs in (1, 2, 3, 7):
+            prob = presets.make_ref_T(k, precision=precision)
+            prob.set_spots([0, 4, -3], [0, 2, 5], [101, 70, 60])
+            prob.thermal.plain_launches = plain
+            if with_map:
+                prob.set_material_map(mm)
+            res[n_slabs] = ctx.heat(prob.thermal, Q, prob.traj, snapshot_legs=[1, 2], n_slabs=n_slabs)
+        assert res[1]["steps_done"] == 231
+        assert np.abs(res[1]["snapshots"][1] - res[1]["snapshots"][0]).max() > 0   # the source heats
+        for n_slabs in (2, 3, 7):
+            for key in ("T", "dose", "snapshots"):
+                np.testing.assert_array_equal(res[n_slabs][key], res[1][key],
+                                              err_msg="%d slabs, %s, map %s" % (n_slabs, key, with_map))
+
+
+def test_heat_slab_count_checked(ctx):
+    k, prob, sx, sy, Q = mini()
+    with pytest.raises(api.BDError):
+        ctx.heat(prob.thermal, Q, prob.traj, n_slabs=prob.thermal.nz)   # fewer than 2 planes per slab
