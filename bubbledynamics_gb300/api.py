@@ -85,6 +85,7 @@ def load(path=None):
                                             C.POINTER(C.c_double)])
     _sig(L, "bd_heat_run_device_noalloc", [P, P, P, P, P, P, C.c_int64, P])
     _sig(L, "bd_westervelt_adjoint", [P, P, P, P, P, P, C.POINTER(C.c_double), P, P, P])
+    _sig(L, "bd_westervelt_adjoint_slabs", [P, P, P, P, P, P, C.c_int32, C.POINTER(C.c_double), P, P, P])
     _sig(L, "bd_write_q_bin", [C.c_char_p, P, C.c_int32, C.c_int32, C.c_int32, C.c_int32])
     _sig(L, "bd_read_q_bin", [C.c_char_p, P, C.c_int64, C.POINTER(C.c_int64)])
     _sig(L, "bd_write_q_axis_dat", [C.c_char_p, P, C.c_int32, C.c_int32, C.c_int32, C.c_double, C.c_double,
@@ -273,19 +274,26 @@ class Context:
         """Session over the planes [z_begin, z_end) of prob (bd_westervelt_slab_begin)."""
         return WesterveltSession(self, prob, slab=(int(z_begin), int(z_end)))
 
-    def westervelt_adjoint(self, prob: WesterveltProblem, loss):
+    def westervelt_adjoint(self, prob: WesterveltProblem, loss, n_slabs=1):
         """Loss of `loss` (abi.FocalLoss) and its gradient w.r.t. the element
         phases and amplitudes of prob's BD_SRC_ARRAY source
-        (bd_westervelt_adjoint).  Returns (loss, grad_phase, grad_amp, timings)
-        with timings = {"forward_ms", "recompute_ms", "backward_ms"}."""
+        (bd_westervelt_adjoint; n_slabs > 1: bd_westervelt_adjoint_slabs, the
+        same bits from that many z slabs).  Returns (loss, grad_phase,
+        grad_amp, timings) with timings = {"forward_ms", "recompute_ms",
+        "backward_ms"}."""
         ne = prob.source.n_elements
         gp = np.zeros(ne, np.float64)
         ga = np.zeros(ne, np.float64)
         tm = np.zeros(3, np.float64)
         L = C.c_double(0.0)
-        check(self.L.bd_westervelt_adjoint(self.h, C.byref(prob.grid), C.byref(prob.medium), C.byref(prob.source),
-                                           C.byref(prob.params), C.byref(loss), C.byref(L), _ptr(gp), _ptr(ga),
-                                           _ptr(tm)))
+        if n_slabs == 1:
+            check(self.L.bd_westervelt_adjoint(self.h, C.byref(prob.grid), C.byref(prob.medium),
+                                               C.byref(prob.source), C.byref(prob.params), C.byref(loss), C.byref(L),
+                                               _ptr(gp), _ptr(ga), _ptr(tm)))
+        else:
+            check(self.L.bd_westervelt_adjoint_slabs(self.h, C.byref(prob.grid), C.byref(prob.medium),
+                                                     C.byref(prob.source), C.byref(prob.params), C.byref(loss),
+                                                     int(n_slabs), C.byref(L), _ptr(gp), _ptr(ga), _ptr(tm)))
         return L.value, gp, ga, {"forward_ms": tm[0], "recompute_ms": tm[1], "backward_ms": tm[2]}
 
     # ------------------------------------------------------------ heat

@@ -1104,7 +1104,7 @@ static void ck_load(WvSession& S, const void* blob, size_t bytes) {
 
 // ---------------------------------------------------------------- adjoint
 template <class real, int NR>
-static void adj_launch_n(WvSession& S, const AdjArgs<real>& a, cudaStream_t st) {
+static void adj_launch_n(WvSession& S, const AdjArgs<real>& a, cudaStream_t st, int part) {
     const WvConst<real>* K = S.kconst.as<WvConst<real>>();
     constexpr int VEC = 16 / sizeof(real);
     if constexpr (sizeof(real) == 4) {
@@ -1115,6 +1115,12 @@ static void adj_launch_n(WvSession& S, const AdjArgs<real>& a, cudaStream_t st) 
             return;
         }
     }
+    if (part == 2) {                          // the stencil pass alone
+        dim3 b(32, 8), g((S.nx + 31) / 32, (S.ny + 7) / 8, (S.nz + a.zb - 1) / a.zb);
+        adj_stencil_kernel<real><<<g, b, 0, st>>>(a);
+        BD_LAUNCHED(S.ctx);
+        return;
+    }
     if (S.nx % VEC == 0) {
         const long long nv = (long long)S.ncell / VEC;
         adj_point_kernel<real, NR, VEC><<<(unsigned)((nv + 255) / 256), 256, 0, st>>>(a, K);
@@ -1122,19 +1128,84 @@ static void adj_launch_n(WvSession& S, const AdjArgs<real>& a, cudaStream_t st) 
         adj_point_kernel<real, NR, 1><<<(unsigned)((S.ncell + 255) / 256), 256, 0, st>>>(a, K);
     }
     BD_LAUNCHED(S.ctx);
+    if (part == 1) return;                    // the pointwise pass alone
     dim3 b(32, 8), g((S.nx + 31) / 32, (S.ny + 7) / 8, (S.nz + a.zb - 1) / a.zb);
     adj_stencil_kernel<real><<<g, b, 0, st>>>(a);
     BD_LAUNCHED(S.ctx);
 }
 
+// One backward step: part 0 = every pass, 1 = the pointwise pass, 2 = the
+// stencil pass (the two-pass path; the fused path is one kernel whatever part)
 template <class real>
-static void adj_launch(WvSession& S, const AdjArgs<real>& a, cudaStream_t st) {
+static void adj_launch(WvSession& S, const AdjArgs<real>& a, cudaStream_t st, int part = 0) {
     switch (S.max_relax) {
-        case 0: adj_launch_n<real, 0>(S, a, st); break;
-        case 1: adj_launch_n<real, 1>(S, a, st); break;
-        case 2: adj_launch_n<real, 2>(S, a, st); break;
-        default: adj_launch_n<real, BD_MAX_RELAX>(S, a, st); break;
+        case 0: adj_launch_n<real, 0>(S, a, st, part); break;
+        case 1: adj_launch_n<real, 1>(S, a, st, part); break;
+        case 2: adj_launch_n<real, 2>(S, a, st, part); break;
+        default: adj_launch_n<real, BD_MAX_RELAX>(S, a, st, part); break;
     }
+}
+
+// loss = sum_x w_L(x) E(x) over the whole grid's energy map, in z-y-x order
+template <class real>
+static double focal_loss_sum(const std::vector<real>& E, int nx, int ny, int nz, const bd_focal_loss* loss) {
+    const int fr2 = loss->focal_radius * loss->focal_radius, sr2 = loss->side_radius * loss->side_radius;
+    double L = 0.0;
+    for (int iz = 0; iz < nz; ++iz)
+        for (int iy = 0; iy < ny; ++iy)
+            for (int ix = 0; ix < nx; ++ix) {
+                const int dx = ix - loss->focus_ix, dy = iy - loss->focus_iy, dz = iz - loss->focus_iz;
+                const int r2 = dx * dx + dy * dy + dz * dz;
+                double wl = 0.0;
+                if (r2 <= fr2) wl = -1.0;
+                else if (iz == loss->focus_iz && r2 >= sr2) wl = loss->side_weight;
+                if (wl != 0.0) L += wl * (double)E[((size_t)iz * ny + iy) * nx + ix];
+            }
+    return L;
+}
+
+// Arguments of the backward kernels that come from the session and the loss
+// (grid, materials, sponge, source tables, loss region); the buffers of the
+// adjoint rings, H and the gradients are the caller's.
+template <class real>
+static void fill_adj_args(const WvSession& S, const bd_focal_loss* loss, AdjArgs<real>& a) {
+    std::memset(&a, 0, sizeof a);
+    a.nx = S.nx; a.ny = S.ny; a.nz = S.nz; a.plane = S.plane;
+    a.max_relax = S.max_relax;
+    a.cmap = S.has_cmap ? S.cmap.as<float>() : nullptr;
+    a.matmap = S.has_matmap ? S.matmap.as<uint8_t>() : nullptr;
+    a.plane_mat = S.has_planemat ? S.planemat.as<int>() : nullptr;
+    if (S.g.sponge_cells > 0) { a.wx = S.wx.as<real>(); a.wy = S.wy.as<real>(); a.wz = S.wz.as<real>(); }
+    a.kxy180 = (real)(S.g.dt * S.g.dt / (S.g.dx * S.g.dx) / 180.0);
+    a.kz180 = (real)(S.g.dt * S.g.dt / (S.g.dz * S.g.dz) / 180.0);
+    a.dt2 = (real)(S.g.dt * S.g.dt);
+    a.dt = (real)S.g.dt;
+    a.relax_scheme = S.p.relax_scheme;
+    a.src_iz = (S.s.kind != BD_SRC_NONE) ? S.s.plane_iz : -1;
+    {
+        // stencil pass: about four waves of 8 CTAs per SM
+        const long long tiles = (long long)((S.nx + 31) / 32) * ((S.ny + 7) / 8);
+        const long long target = 32LL * S.ctx->sm_count;
+        a.zb = (int)std::min<long long>(64, std::max<long long>(4, (tiles * S.nz + target - 1) / target));
+    }
+    a.sAf = S.sAf.as<float>(); a.sPsi = S.sPsi.as<float>(); a.sTauf = S.sTauf.as<float>();
+    a.theta = S.theta.as<float>(); a.tb0 = S.tb0.as<float>();
+    a.sA = S.sA.as<double>(); a.sVar = S.sVar.as<double>(); a.sTau = S.sTau.as<double>(); a.sPhi = S.sPhi.as<double>();
+    a.t_src = S.t_src.as<double>();
+    a.n_tones = S.s.n_tones;
+    a.burst = S.s.burst_cycles > 0.0;
+    for (int k = 0; k < BD_MAX_TONES; ++k) {
+        a.freq[k] = S.s.freq[k]; a.tamp[k] = S.s.amp[k]; a.tphase[k] = S.s.phase[k]; a.tampf[k] = (float)S.s.amp[k];
+    }
+    a.tau_max = S.tau_max;
+    a.burst_len = a.burst ? S.s.burst_cycles / S.s.freq[0] : 0.0;
+    a.burst_lenf = (float)a.burst_len;
+    a.fx = loss->focus_ix; a.fy = loss->focus_iy; a.fz = loss->focus_iz - S.zoff;
+    a.frad2 = loss->focal_radius * loss->focal_radius;
+    a.srad2 = loss->side_radius * loss->side_radius;
+    a.side_w = loss->side_weight;
+    a.win0 = loss->window_start;
+    a.win1 = loss->window_end;
 }
 
 template <class real>
@@ -1265,21 +1336,9 @@ static void adjoint_solve(WvSession& S, const bd_focal_loss* loss, double* loss_
     BD_CUDA(cudaEventSynchronize(S.ctx->ev1));
     float ms_fwd = 0;
     BD_CUDA(cudaEventElapsedTime(&ms_fwd, S.ctx->ev0, S.ctx->ev1));
-    // loss = sum_x w_L(x) E(x)
     std::vector<real> E(S.ncell);
     BD_CUDA(cudaMemcpy(E.data(), S.energy.p, f, cudaMemcpyDeviceToHost));
-    const int fr2 = loss->focal_radius * loss->focal_radius, sr2 = loss->side_radius * loss->side_radius;
-    double L = 0.0;
-    for (int iz = 0; iz < S.nz; ++iz)
-        for (int iy = 0; iy < S.ny; ++iy)
-            for (int ix = 0; ix < S.nx; ++ix) {
-                const int dx = ix - loss->focus_ix, dy = iy - loss->focus_iy, dz = iz - loss->focus_iz;
-                const int r2 = dx * dx + dy * dy + dz * dz;
-                double wl = 0.0;
-                if (r2 <= fr2) wl = -1.0;
-                else if (iz == loss->focus_iz && r2 >= sr2) wl = loss->side_weight;
-                if (wl != 0.0) L += wl * (double)E[((size_t)iz * S.ny + iy) * S.nx + ix];
-            }
+    const double L = focal_loss_sum(E, S.nx, S.ny, S.nz, loss);
     if (loss_out) *loss_out = L;
     // backward buffers
     PoolBuf mu[6], muR[BD_MAX_RELAX][3], gphi, gamp, eamp, Hb[2];
@@ -1318,42 +1377,10 @@ static void adjoint_solve(WvSession& S, const bd_focal_loss* loss, double* loss_
     const int n_dft_saved = S.n_dft;
     S.n_dft = 0;
     AdjArgs<real> a;
-    std::memset(&a, 0, sizeof a);
-    a.nx = S.nx; a.ny = S.ny; a.nz = S.nz; a.plane = S.plane;
-    a.max_relax = S.max_relax;
-    a.cmap = S.has_cmap ? S.cmap.as<float>() : nullptr;
-    a.matmap = S.has_matmap ? S.matmap.as<uint8_t>() : nullptr;
-    a.plane_mat = S.has_planemat ? S.planemat.as<int>() : nullptr;
-    if (S.g.sponge_cells > 0) { a.wx = S.wx.as<real>(); a.wy = S.wy.as<real>(); a.wz = S.wz.as<real>(); }
-    a.kxy180 = (real)(S.g.dt * S.g.dt / (S.g.dx * S.g.dx) / 180.0);
-    a.kz180 = (real)(S.g.dt * S.g.dt / (S.g.dz * S.g.dz) / 180.0);
-    a.dt2 = (real)(S.g.dt * S.g.dt);
-    a.dt = (real)S.g.dt;
-    a.relax_scheme = S.p.relax_scheme;
-    a.src_iz = (S.s.kind != BD_SRC_NONE) ? S.s.plane_iz : -1;
-    {
-        // stencil pass: about four waves of 8 CTAs per SM
-        const long long tiles = (long long)((S.nx + 31) / 32) * ((S.ny + 7) / 8);
-        const long long target = 32LL * S.ctx->sm_count;
-        a.zb = (int)std::min<long long>(64, std::max<long long>(4, (tiles * S.nz + target - 1) / target));
-        a.H = Hb[0].as<real>();
-        a.Hin = Hb[1].as<real>();
-    }
+    fill_adj_args(S, loss, a);
+    a.H = Hb[0].as<real>();
+    a.Hin = Hb[1].as<real>();
     a.gphi = gphi.as<double>(); a.gamp = gamp.as<double>(); a.e_amp = eamp.as<double>();
-    a.sAf = S.sAf.as<float>(); a.sPsi = S.sPsi.as<float>(); a.sTauf = S.sTauf.as<float>();
-    a.theta = S.theta.as<float>(); a.tb0 = S.tb0.as<float>();
-    a.sA = S.sA.as<double>(); a.sVar = S.sVar.as<double>(); a.sTau = S.sTau.as<double>(); a.sPhi = S.sPhi.as<double>();
-    a.t_src = S.t_src.as<double>();
-    a.n_tones = S.s.n_tones;
-    a.burst = S.s.burst_cycles > 0.0;
-    for (int k = 0; k < BD_MAX_TONES; ++k) {
-        a.freq[k] = S.s.freq[k]; a.tamp[k] = S.s.amp[k]; a.tphase[k] = S.s.phase[k]; a.tampf[k] = (float)S.s.amp[k];
-    }
-    a.tau_max = S.tau_max;
-    a.burst_len = a.burst ? S.s.burst_cycles / S.s.freq[0] : 0.0;
-    a.burst_lenf = (float)a.burst_len;
-    a.fx = loss->focus_ix; a.fy = loss->focus_iy; a.fz = loss->focus_iz;
-    a.frad2 = fr2; a.srad2 = sr2; a.side_w = loss->side_weight;
     // backward step counter on the device: forward index of the next backward step
     PoolBuf bstep;
     bstep.alloc(S.ctx, 64);
@@ -1363,8 +1390,6 @@ static void adjoint_solve(WvSession& S, const bd_focal_loss* loss, double* loss_
         BD_CUDA(cudaStreamSynchronize(st));
     }
     a.bstep = bstep.as<long long>();
-    a.win0 = loss->window_start;
-    a.win1 = loss->window_end;
     // backward steps s1-1 .. s0 of a segment after nb earlier backward steps
     auto backward_steps = [&](cudaStream_t cs, int64_t s0, int64_t s1, int64_t nb) {
         int rot = (int)(nb % 6), rrot = (int)(nb % 3);    // rotation of the adjoint rings
@@ -1439,6 +1464,264 @@ static void adjoint_solve(WvSession& S, const bd_focal_loss* loss, double* loss_
     if (grad_phase) for (int e = 0; e < ne; ++e) grad_phase[e] = 0.0;
     if (grad_amp) for (int e = 0; e < ne; ++e) grad_amp[e] = 0.0;
     for (long long j = 0; j < S.plane; ++j) {
+        const int e = elem[j];
+        if (e < 0) continue;
+        if (grad_phase) grad_phase[e] += gp[j];
+        if (grad_amp) grad_amp[e] += ga[j];
+    }
+    if (timings) { timings[0] = ms_fwd; timings[1] = ms_rec; timings[2] = ms_bwd; }
+}
+
+
+// Levels of a session at step s: k < 5: p^{s-k}; 5 + 2v + j: R^{s-1-j} of process v.
+static PoolBuf& adj_level(WvSession& S, int64_t s, int k) {
+    if (k < 5) return S.P[(head_of(s) + k) % 5];
+    const int v = (k - 5) / 2, j = (k - 5) % 2;
+    return S.R[v][(int)(s & 1) ^ j];
+}
+
+// kHalo planes of two buffers of neighbouring slabs: the lower slab's top owned
+// planes to the upper slab's low ghost planes, the upper slab's bottom owned
+// planes to the lower slab's high ghost planes.
+static void exchange_planes(const WvSession& lo, const WvSession& hi, void* lb, void* hb, cudaStream_t st) {
+    const size_t pb = (size_t)lo.plane * lo.esz;
+    char* L = static_cast<char*>(lb);
+    char* H = static_cast<char*>(hb);
+    BD_CUDA(cudaMemcpyAsync(H + (size_t)(hi.own0 - kHalo) * pb, L + (size_t)(lo.own1 - kHalo) * pb, kHalo * pb,
+                            cudaMemcpyDeviceToDevice, st));
+    BD_CUDA(cudaMemcpyAsync(L + (size_t)lo.own1 * pb, H + (size_t)hi.own0 * pb, kHalo * pb, cudaMemcpyDeviceToDevice,
+                            st));
+}
+
+// The adjoint solve over K z slabs of one device: the z-slab split of a
+// multi-GPU gradient (each slab its own fields, checkpoints, adjoint rings and
+// H), checked against the one-domain solve.  Forward and recompute steps
+// exchange the 3 ghost planes of p^n after every step like the slab forward
+// solve; a backward step couples planes only through the transposed stencil of
+// H, so after every step the ghost planes of that step's H take the
+// neighbours' owned planes (between the pointwise and stencil passes on the
+// two-pass path).  Every other backward quantity is pointwise: ghost planes
+// compute values nobody reads.  Only the slab that owns the source plane adds
+// to the source gradient, and the loss is summed over the whole grid in the
+// one-domain order, so loss and gradients are the one-domain bits.  Steps go
+// out as plain launches, slab after slab.
+template <class real>
+static void adjoint_solve_slabs(std::vector<WvSession*>& sl, const bd_focal_loss* loss, double* loss_out,
+                                double* grad_phase, double* grad_amp, double* timings) {
+    const int K = (int)sl.size();
+    WvSession& S0 = *sl[0];
+    bd_context* ctx = S0.ctx;
+    cudaStream_t st = ctx->stream;
+    const int64_t N = S0.p.n_steps;
+    const int64_t sqrtN = std::max<int64_t>(1, (int64_t)std::ceil(std::sqrt((double)N)));
+    int64_t Kc = loss->checkpoint_every > 0 ? std::min<int64_t>(loss->checkpoint_every, N) : sqrtN;
+    if (loss->checkpoint_every < 0) {
+        size_t fr = 0, tot = 0, fsum = 0;
+        BD_CUDA(cudaMemGetInfo(&fr, &tot));
+        for (auto* S : sl) fsum += S->ncell * S->esz;
+        if ((double)(N + 5) * (double)fsum <= 0.5 * ((double)fr + (double)ctx->pool_bytes)) Kc = N;
+    }
+    const int64_t nck = (N + Kc - 1) / Kc;
+    const int nlev = 5 + 2 * S0.max_relax;
+    // the slab that owns the source plane
+    int ko = -1;
+    for (int k = 0; k < K; ++k)
+        if (sl[k]->s.kind != BD_SRC_NONE && sl[k]->s.plane_iz >= sl[k]->own0 && sl[k]->s.plane_iz < sl[k]->own1) ko = k;
+    if (ko < 0) fail(BD_ERR_INVALID_ARG, "no slab owns the source plane");
+    struct Per {
+        std::vector<PoolBuf> ck, seg;
+        PoolBuf mu[6], muR[BD_MAX_RELAX][3], gphi, gamp, eamp, Hb[2];
+        AdjArgs<real> a;
+        size_t f = 0;
+    };
+    std::vector<Per> per(K);
+    for (int k = 0; k < K; ++k) {
+        Per& P = per[k];
+        P.f = sl[k]->ncell * sl[k]->esz;
+        P.ck.resize((nck - 1) * nlev);
+        for (auto& b : P.ck) b.alloc(ctx, P.f);
+        P.seg.resize(Kc + 5);
+        for (auto& b : P.seg) b.alloc(ctx, P.f);
+    }
+    auto forward_step = [&]() {
+        for (auto* S : sl) {
+            issue_steps(*S, S->variant, S->step, 1, st);
+            S->step += 1;
+        }
+        for (int k = 0; k + 1 < K; ++k) halo_exchange(*sl[k], *sl[k + 1], st);
+    };
+    // levels p^{s0-4} .. p^{s1} of every slab into its segment store
+    auto store_segment = [&](int64_t s0, int64_t s1) {
+        for (int k = 0; k < K; ++k)
+            for (int j = 0; j < 5; ++j)
+                BD_CUDA(cudaMemcpyAsync(per[k].seg[4 - j].p, adj_level(*sl[k], s0, j).p, per[k].f,
+                                        cudaMemcpyDeviceToDevice, st));
+        for (int64_t s = s0; s < s1; ++s) {
+            forward_step();
+            for (int k = 0; k < K; ++k)
+                BD_CUDA(cudaMemcpyAsync(per[k].seg[s - s0 + 5].p, sl[k]->P[head_of(s + 1)].p, per[k].f,
+                                        cudaMemcpyDeviceToDevice, st));
+        }
+    };
+    BD_CUDA(cudaEventRecord(ctx->ev0, st));
+    for (int64_t c = 0; c < nck; ++c) {
+        const int64_t s0 = c * Kc, s1 = std::min<int64_t>(N, s0 + Kc);
+        if (c + 1 < nck) {
+            for (int k = 0; k < K; ++k)
+                for (int j = 0; j < nlev; ++j)
+                    BD_CUDA(cudaMemcpyAsync(per[k].ck[c * nlev + j].p, adj_level(*sl[k], s0, j).p, per[k].f,
+                                            cudaMemcpyDeviceToDevice, st));
+            for (int64_t s = s0; s < s1; ++s) forward_step();
+        } else {
+            store_segment(s0, s1);
+        }
+    }
+    BD_CUDA(cudaEventRecord(ctx->ev1, st));
+    BD_CUDA(cudaEventSynchronize(ctx->ev1));
+    float ms_fwd = 0;
+    BD_CUDA(cudaEventElapsedTime(&ms_fwd, ctx->ev0, ctx->ev1));
+    // the whole grid's energy map from the owned planes, summed in the one-domain order
+    const int nz = S0.nz_glob;
+    std::vector<real> E((size_t)S0.plane * nz);
+    for (auto* S : sl)
+        BD_CUDA(cudaMemcpy(E.data() + (size_t)(S->zoff + S->own0) * S->plane,
+                           static_cast<const real*>(S->energy.p) + (size_t)S->own0 * S->plane,
+                           (size_t)(S->own1 - S->own0) * S->plane * sizeof(real), cudaMemcpyDeviceToHost));
+    const double L = focal_loss_sum(E, S0.nx, S0.ny, nz, loss);
+    if (loss_out) *loss_out = L;
+    // per-element amplitude of every source-plane cell (the owning slab's source)
+    const WvSession& So = *sl[ko];
+    std::vector<double> ea(So.plane, 0.0);
+    std::vector<int> elem(So.plane, -1);
+    for (long long j = 0; j < So.plane; ++j) {
+        if (So.s.kind == BD_SRC_ARRAY) {
+            const int e = So.s.element_of_cell[j];
+            if (e >= 0 && e < So.s.n_elements) { elem[j] = e; ea[j] = So.s.element_amp ? So.s.element_amp[e] : 1.0; }
+        } else {
+            ea[j] = 1.0;
+        }
+    }
+    const bool fused = S0.prec == BD_F32 && S0.nx % 4 == 0;
+    PoolBuf bstep;
+    bstep.alloc(ctx, 64);
+    {
+        const long long last = N - 1;
+        BD_CUDA(cudaMemcpyAsync(bstep.p, &last, sizeof last, cudaMemcpyHostToDevice, st));
+        BD_CUDA(cudaStreamSynchronize(st));
+    }
+    std::vector<bd_westervelt_params> saved(K);
+    std::vector<int> n_dft_saved(K);
+    for (int k = 0; k < K; ++k) {
+        WvSession& S = *sl[k];
+        Per& P = per[k];
+        S.adj_fused = fused;
+        for (auto& b : P.Hb) { b.alloc(ctx, P.f); BD_CUDA(cudaMemsetAsync(b.p, 0, P.f, st)); }
+        for (auto& b : P.mu) { b.alloc(ctx, P.f); BD_CUDA(cudaMemsetAsync(b.p, 0, P.f, st)); }
+        for (int v = 0; v < S.max_relax; ++v)
+            for (auto& b : P.muR[v]) { b.alloc(ctx, P.f); BD_CUDA(cudaMemsetAsync(b.p, 0, P.f, st)); }
+        P.gphi.alloc(ctx, S.plane * 8); P.gamp.alloc(ctx, S.plane * 8);
+        BD_CUDA(cudaMemsetAsync(P.gphi.p, 0, S.plane * 8, st));
+        BD_CUDA(cudaMemsetAsync(P.gamp.p, 0, S.plane * 8, st));
+        upload(S, P.eamp, ea);
+        // the recompute runs without accumulators
+        saved[k] = S.p;
+        n_dft_saved[k] = S.n_dft;
+        S.p.peak_end = S.p.peak_start;
+        S.p.energy_end = S.p.energy_start;
+        S.p.dft_len = 0;
+        S.n_dft = 0;
+        fill_adj_args(S, loss, P.a);
+        if (k != ko) P.a.src_iz = -1;           // a ghost copy of the source plane adds no gradient
+        P.a.H = P.Hb[0].as<real>();
+        P.a.Hin = P.Hb[1].as<real>();
+        P.a.gphi = P.gphi.as<double>(); P.a.gamp = P.gamp.as<double>(); P.a.e_amp = P.eamp.as<double>();
+        P.a.bstep = bstep.as<long long>();
+    }
+    struct Restore {
+        std::vector<WvSession*>& sl;
+        std::vector<bd_westervelt_params>& p;
+        std::vector<int>& nd;
+        ~Restore() {
+            for (size_t k = 0; k < sl.size(); ++k) { sl[k]->p = p[k]; sl[k]->n_dft = nd[k]; sl[k]->adj_fused = false; }
+        }
+    } restore{sl, saved, n_dft_saved};
+    int64_t nb_done = 0;
+    float ms_rec = 0, ms_bwd = 0;
+    for (int64_t c = nck - 1; c >= 0; --c) {
+        const int64_t s0 = c * Kc, s1 = std::min<int64_t>(N, s0 + Kc);
+        BD_CUDA(cudaEventRecord(ctx->ev0, st));
+        if (c + 1 < nck) {
+            for (int k = 0; k < K; ++k) {
+                WvSession& S = *sl[k];
+                for (int j = 0; j < nlev; ++j)
+                    BD_CUDA(cudaMemcpyAsync(adj_level(S, s0, j).p, per[k].ck[c * nlev + j].p, per[k].f,
+                                            cudaMemcpyDeviceToDevice, st));
+                long long sb = s0;
+                BD_CUDA(cudaMemcpyAsync(S.step_base.p, &sb, sizeof sb, cudaMemcpyHostToDevice, st));
+                BD_CUDA(cudaStreamSynchronize(st));
+                S.step = s0;
+            }
+            store_segment(s0, s1);
+        }
+        BD_CUDA(cudaEventRecord(ctx->ev1, st));
+        int rot = (int)(nb_done % 6), rrot = (int)(nb_done % 3);
+        int koff = 0;
+        for (int64_t s = s1 - 1; s >= s0; --s, ++koff) {
+            for (int part = fused ? 0 : 1; part <= (fused ? 0 : 2); ++part) {
+                for (int k = 0; k < K; ++k) {
+                    WvSession& S = *sl[k];
+                    Per& P = per[k];
+                    AdjArgs<real> a = P.a;
+                    for (int j = 0; j < 5; ++j) a.mu[j] = P.mu[(rot + j) % 6].as<real>();
+                    a.mu5 = P.mu[(rot + 5) % 6].as<real>();
+                    for (int v = 0; v < S.max_relax; ++v) {
+                        a.muR1[v] = P.muR[v][rrot].as<real>();
+                        a.muR2[v] = P.muR[v][(rrot + 1) % 3].as<real>();
+                        a.muR3[v] = P.muR[v][(rrot + 2) % 3].as<real>();
+                    }
+                    for (int j = 0; j < 5; ++j) a.fp[j] = P.seg[s - s0 + 5 - j].as<real>();
+                    if (fused) {
+                        a.H = P.Hb[s & 1].as<real>();            // written by this step
+                        a.Hin = P.Hb[(s + 1) & 1].as<real>();    // written by step s + 1
+                    }
+                    a.koff = koff;
+                    adj_launch<real>(S, a, st, part);
+                }
+                if (part != 2)                  // H of this step: ghost planes from the neighbours
+                    for (int k = 0; k + 1 < K; ++k) {
+                        const int hb = fused ? (int)(s & 1) : 0;
+                        exchange_planes(*sl[k], *sl[k + 1], per[k].Hb[hb].p, per[k + 1].Hb[hb].p, st);
+                    }
+            }
+            rot = (rot + 1) % 6;
+            rrot = (rrot + 1) % 3;
+        }
+        adj_advance_kernel<<<1, 32, 0, st>>>(bstep.as<long long>(), (int)(s1 - s0));
+        BD_LAUNCHED(ctx);
+        nb_done += s1 - s0;
+        cudaEvent_t e2;
+        BD_CUDA(cudaEventCreate(&e2));
+        BD_CUDA(cudaEventRecord(e2, st));
+        BD_CUDA(cudaEventSynchronize(e2));
+        float m1 = 0, m2 = 0;
+        BD_CUDA(cudaEventElapsedTime(&m1, ctx->ev0, ctx->ev1));
+        BD_CUDA(cudaEventElapsedTime(&m2, ctx->ev1, e2));
+        cudaEventDestroy(e2);
+        ms_rec += m1;
+        ms_bwd += m2;
+    }
+    for (auto* S : sl) {
+        unsigned fl = 0;
+        BD_CUDA(cudaMemcpy(&fl, S->flag.as<unsigned>() + 1, sizeof fl, cudaMemcpyDeviceToHost));
+        if (fl & 4u) fail(BD_ERR_TIMEOUT, "a pipeline wait of the adjoint solve timed out");
+    }
+    std::vector<double> gp(So.plane), ga(So.plane);
+    BD_CUDA(cudaMemcpy(gp.data(), per[ko].gphi.p, So.plane * 8, cudaMemcpyDeviceToHost));
+    BD_CUDA(cudaMemcpy(ga.data(), per[ko].gamp.p, So.plane * 8, cudaMemcpyDeviceToHost));
+    const int ne = So.s.kind == BD_SRC_ARRAY ? So.s.n_elements : 0;
+    if (grad_phase) for (int e = 0; e < ne; ++e) grad_phase[e] = 0.0;
+    if (grad_amp) for (int e = 0; e < ne; ++e) grad_amp[e] = 0.0;
+    for (long long j = 0; j < So.plane; ++j) {
         const int e = elem[j];
         if (e < 0) continue;
         if (grad_phase) grad_phase[e] += gp[j];
@@ -1595,29 +1878,64 @@ bd_status bd_checkpoint_load(bd_westervelt* w, const void* blob, size_t bytes) {
     });
 }
 
+// Checks of the adjoint's arguments and the forward parameters it runs with.
+static bd_westervelt_params adjoint_params(const bd_grid* grid, const bd_source* source,
+                                           const bd_westervelt_params* params, const bd_focal_loss* loss) {
+    if (!grid || !loss || !params) fail(BD_ERR_INVALID_ARG, "null argument");
+    for (int f = 0; f < 6; ++f)
+        if (grid->face[f] != BD_FACE_OPEN) fail(BD_ERR_UNSUPPORTED, "the adjoint supports OPEN faces only");
+    if (!source || source->kind == BD_SRC_NONE) fail(BD_ERR_INVALID_ARG, "the adjoint needs a source");
+    if (loss->window_start < 0 || loss->window_end > params->n_steps || loss->window_start >= loss->window_end)
+        fail(BD_ERR_INVALID_ARG, "bad loss window");
+    bd_westervelt_params p = *params;
+    p.energy_mode = BD_ENERGY_P2;
+    p.energy_start = loss->window_start;
+    p.energy_end = loss->window_end;
+    p.peak_start = p.peak_end = 0;
+    p.n_dft = 0;
+    p.q_mode = BD_Q_NONE;
+    p.fault_at_step = -1;
+    return p;
+}
+
 bd_status bd_westervelt_adjoint(bd_context* ctx, const bd_grid* grid, const bd_medium* medium, const bd_source* source,
                                 const bd_westervelt_params* params, const bd_focal_loss* loss, double* loss_out,
                                 double* grad_phase, double* grad_amp, double* timings_ms) {
     return guard([&] {
         ctx_check(ctx);
-        if (!grid || !loss || !params) fail(BD_ERR_INVALID_ARG, "null argument");
-        for (int f = 0; f < 6; ++f)
-            if (grid->face[f] != BD_FACE_OPEN) fail(BD_ERR_UNSUPPORTED, "the adjoint supports OPEN faces only");
-        if (!source || source->kind == BD_SRC_NONE) fail(BD_ERR_INVALID_ARG, "the adjoint needs a source");
-        if (loss->window_start < 0 || loss->window_end > params->n_steps || loss->window_start >= loss->window_end)
-            fail(BD_ERR_INVALID_ARG, "bad loss window");
-        bd_westervelt_params p = *params;
-        p.energy_mode = BD_ENERGY_P2;
-        p.energy_start = loss->window_start;
-        p.energy_end = loss->window_end;
-        p.peak_start = p.peak_end = 0;
-        p.n_dft = 0;
-        p.q_mode = BD_Q_NONE;
-        p.fault_at_step = -1;
+        const bd_westervelt_params p = adjoint_params(grid, source, params, loss);
         bd_westervelt w;
         setup(w.S, ctx, grid, medium, source, &p);
         if (w.S.prec == BD_F32) adjoint_solve<float>(w.S, loss, loss_out, grad_phase, grad_amp, timings_ms);
         else adjoint_solve<double>(w.S, loss, loss_out, grad_phase, grad_amp, timings_ms);
+    });
+}
+
+bd_status bd_westervelt_adjoint_slabs(bd_context* ctx, const bd_grid* grid, const bd_medium* medium,
+                                      const bd_source* source, const bd_westervelt_params* params,
+                                      const bd_focal_loss* loss, int32_t n_slabs, double* loss_out,
+                                      double* grad_phase, double* grad_amp, double* timings_ms) {
+    return guard([&] {
+        ctx_check(ctx);
+        const bd_westervelt_params p = adjoint_params(grid, source, params, loss);
+        if (n_slabs < 1 || n_slabs > grid->nz / 8) fail(BD_ERR_INVALID_ARG, "n_slabs must be 1..nz/8");
+        if (n_slabs == 1) {
+            bd_westervelt w;
+            setup(w.S, ctx, grid, medium, source, &p);
+            if (w.S.prec == BD_F32) adjoint_solve<float>(w.S, loss, loss_out, grad_phase, grad_amp, timings_ms);
+            else adjoint_solve<double>(w.S, loss, loss_out, grad_phase, grad_amp, timings_ms);
+            return;
+        }
+        std::vector<std::unique_ptr<WvSession>> own;
+        std::vector<WvSession*> sl;
+        for (int k = 0; k < n_slabs; ++k) {
+            own.emplace_back(new WvSession());
+            setup_slab(*own[k], ctx, grid, medium, source, &p, (int)((long long)grid->nz * k / n_slabs),
+                       (int)((long long)grid->nz * (k + 1) / n_slabs));
+            sl.push_back(own[k].get());
+        }
+        if (sl[0]->prec == BD_F32) adjoint_solve_slabs<float>(sl, loss, loss_out, grad_phase, grad_amp, timings_ms);
+        else adjoint_solve_slabs<double>(sl, loss, loss_out, grad_phase, grad_amp, timings_ms);
     });
 }
 

@@ -302,6 +302,16 @@ bd_status bd_westervelt_adjoint(bd_context* ctx, const bd_grid* grid, const bd_m
                                 const bd_source* source, const bd_westervelt_params* params,
                                 const bd_focal_loss* loss, double* loss_out,
                                 double* grad_phase, double* grad_amp, double* timings_ms);
+/* The same gradient computed on n_slabs z slabs of this context's device (the
+ * z-slab split of a multi-GPU adjoint, each slab its own fields, checkpoints
+ * and adjoint rings): 3 ghost planes of p^n exchanged after every forward and
+ * recompute step, of H (the only field the backward stencil couples) after
+ * every backward step; loss and gradients equal bd_westervelt_adjoint's bit
+ * for bit.  1 <= n_slabs <= nz / 8; plain launches (no graphs). */
+bd_status bd_westervelt_adjoint_slabs(bd_context* ctx, const bd_grid* grid, const bd_medium* medium,
+                                      const bd_source* source, const bd_westervelt_params* params,
+                                      const bd_focal_loss* loss, int32_t n_slabs, double* loss_out,
+                                      double* grad_phase, double* grad_amp, double* timings_ms);
 
 /* ------------------------------------------------------------------------- */
 /* Bioheat + CEM43 dose along a scan trajectory (T)                           */

@@ -74,6 +74,31 @@ def test_adjoint_gradient_independent_of_checkpoint_interval(ctx, prec):
 
 
 @pytest.mark.parametrize("prec", [abi.BD_F64, abi.BD_F32])
+def test_adjoint_slabs_equal_single_domain(ctx, prec):
+    """The z-slab split of the gradient: 2, 3 and 4 slabs (each its own fields,
+    checkpoints and adjoint rings; ghost planes of p^n after every forward and
+    recompute step, of H after every backward step) give the one-domain loss
+    and gradients bit for bit, with sqrt(N) checkpoints and with an interval of
+    7.  FP32 runs the fused backward pass, FP64 the pointwise and stencil
+    passes with the exchange between them."""
+    for k in (0, 7):
+        prob, loss = presets.adjoint_mini(precision=prec)
+        loss.checkpoint_every = k
+        ref = ctx.westervelt_adjoint(prob, loss)
+        assert np.abs(ref[1]).max() > 0
+        for n_slabs in (2, 3, 4):
+            prob, loss = presets.adjoint_mini(precision=prec)
+            loss.checkpoint_every = k
+            got = ctx.westervelt_adjoint(prob, loss, n_slabs=n_slabs)
+            assert got[0] == ref[0], (k, n_slabs)
+            np.testing.assert_array_equal(got[1], ref[1], err_msg="phase, K = %d, %d slabs" % (k, n_slabs))
+            np.testing.assert_array_equal(got[2], ref[2], err_msg="amplitude, K = %d, %d slabs" % (k, n_slabs))
+    prob, loss = presets.adjoint_mini(precision=prec)
+    with pytest.raises(api.BDError):
+        ctx.westervelt_adjoint(prob, loss, n_slabs=5)        # fewer than 8 planes per slab
+
+
+@pytest.mark.parametrize("prec", [abi.BD_F64, abi.BD_F32])
 def test_adjoint_graphs_and_plain_launches_identical(ctx, prec):
     """The recompute and backward sweeps replayed as captured CUDA graphs (one
     per segment parity and adjoint-ring rotation) give the bits of plain
