@@ -18,11 +18,14 @@ host (oracle/_ref) on the same grid (its two-layer physics), all host cores.
 --impl reference-gpu times the reference's own CUDA kernels (W's step loop,
 G's DPRK_step one thread per bubble; oracle/_ref/libbdref_gpu.so) beside this
 library on the same problems (the comparison baseline of the speed-ups).
-The default line also carries the cfg3, cfg4, cfg5 and cfg2 summaries and
-the reference's own Westervelt kernels on the GPU (--no-extra skips them).
+The default one-GPU line also carries the cfg3, cfg4, cfg5 and cfg2
+summaries and the reference's own Westervelt kernels on the GPU (--no-extra
+skips them).
 --workload threshold-scale runs G's search over its whole table with capped
 integrations.
---gpus N under torchrun: N independent replicas (the solver does not shard).
+--gpus N under torchrun: N independent replicas of the cfg1 solve (weak
+scaling); the z-slab split of a solve across devices is checked as slabs of
+one device in the tests.
 """
 import argparse
 import json
@@ -282,7 +285,9 @@ def run_westervelt(args, world, rank, local):
         "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk.summary(),
         "gpu_launches": int(launches),
     }
-    if not args.no_extra:
+    if not args.no_extra and world == 1:
+        # the other rows of the measurement ride on the one-GPU line; the
+        # multi-GPU lines carry the replicated cfg1 solve alone
         line["adjoint"] = adjoint_summary(ctx)
         line["cfg3"] = cfg3_summary(ctx)
         line["cfg5"] = cfg5_summary(ctx)
