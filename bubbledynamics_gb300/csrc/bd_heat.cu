@@ -528,16 +528,18 @@ static void heat_run(bd_context* ctx, const bd_thermal* th, const double* Q, con
                 }
             }
         };
-        while (done < nsteps) {
-            int64_t next = nsteps;
-            if (isnap < snaps.size()) next = std::min<int64_t>(next, snaps[isnap].first);
-            if (next > done) run_steps(done, next);
-            done = next;
+        while (true) {
+            // snapshots due at this step (a leg of zero steps ends where it starts)
             while (isnap < snaps.size() && snaps[isnap].first <= done) {
                 if (out->snapshots)
                     copy_T(done, static_cast<double*>(out->snapshots) + (size_t)snaps[isnap].second * n);
                 ++isnap;
             }
+            if (done >= nsteps) break;
+            int64_t next = nsteps;
+            if (isnap < snaps.size()) next = std::min<int64_t>(next, snaps[isnap].first);
+            run_steps(done, next);
+            done = next;
         }
         BD_CUDA(cudaEventRecord(ctx->ev1, s));
         BD_CUDA(cudaEventSynchronize(ctx->ev1));
