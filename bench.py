@@ -288,15 +288,25 @@ def run_westervelt(args, world, rank, local):
     if not args.no_extra and world == 1:
         # the other rows of the measurement ride on the one-GPU line; the
         # multi-GPU lines carry the replicated cfg1 solve alone
-        line["adjoint"] = adjoint_summary(ctx)
-        line["cfg3"] = cfg3_summary(ctx)
-        line["cfg5"] = cfg5_summary(ctx)
-        line["gilmore"] = gilmore_summary(ctx, with_cpu=not args.no_cpu)
+        line["adjoint"] = extra_row(adjoint_summary, ctx)
+        line["cfg3"] = extra_row(cfg3_summary, ctx)
+        line["cfg5"] = extra_row(cfg5_summary, ctx)
+        line["gilmore"] = extra_row(gilmore_summary, ctx, with_cpu=not args.no_cpu)
         # the reference's own W kernels built for this GPU, on the cfg1 grid with its physics
-        line["reference_gpu"] = reference_gpu_summary(ctx, gilmore=False)
+        line["reference_gpu"] = extra_row(reference_gpu_summary, ctx, gilmore=False)
     if rank == 0:
         print(json.dumps(line), flush=True)
     ctx.close()
+
+
+def extra_row(fn, *args, **kw):
+    """One extra measurement row; an exception there is recorded in the row
+    instead of losing the headline line."""
+    try:
+        return fn(*args, **kw)
+    except Exception as e:
+        msg = str(e).splitlines()[0] if str(e) else type(e).__name__
+        return {"error": msg}
 
 
 def adjoint_summary(ctx):
