@@ -19,8 +19,8 @@ host (oracle/_ref) on the same grid (its two-layer physics), all host cores.
 G's DPRK_step one thread per bubble; oracle/_ref/libbdref_gpu.so) beside this
 library on the same problems (the comparison baseline of the speed-ups).
 The default one-GPU line also carries the cfg3, cfg4, cfg5 and cfg2
-summaries and the reference's own Westervelt kernels on the GPU (--no-extra
-skips them).
+summaries and the reference's own Westervelt and Gilmore kernels on the GPU
+beside this library (--no-extra skips them).
 --workload threshold-scale runs G's search over its whole table with capped
 integrations.
 --gpus N under torchrun: N independent replicas of the cfg1 solve (weak
@@ -292,8 +292,9 @@ def run_westervelt(args, world, rank, local):
         line["cfg3"] = extra_row(cfg3_summary, ctx)
         line["cfg5"] = extra_row(cfg5_summary, ctx)
         line["gilmore"] = extra_row(gilmore_summary, ctx, with_cpu=not args.no_cpu)
-        # the reference's own W kernels built for this GPU, on the cfg1 grid with its physics
-        line["reference_gpu"] = extra_row(reference_gpu_summary, ctx, gilmore=False)
+        # the reference's own W and G kernels built for this GPU: W's step loop on
+        # the cfg1 grid with its physics, G's DPRK_step on 2^15 cfg2 bubbles
+        line["reference_gpu"] = extra_row(reference_gpu_summary, ctx)
     if rank == 0:
         print(json.dumps(line), flush=True)
     ctx.close()
