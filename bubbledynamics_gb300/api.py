@@ -75,6 +75,13 @@ def load(path=None):
     _sig(L, "bd_unfold_quarter", [P, C.c_int32, C.c_int32, P])
     _sig(L, "bd_spiral_heat_run", [P, P, P, P, C.c_int64, P])
     _sig(L, "bd_spiral_heat_run_slabs", [P, P, P, P, C.c_int64, C.c_int32, P])
+    _sig(L, "bd_heat_slab_begin", [P, P, P, P, C.c_int64, C.c_int32, C.c_int32, C.POINTER(P)])
+    _sig(L, "bd_heat_slab_steps", [P, C.POINTER(C.c_int64), C.POINTER(C.c_int64)])
+    _sig(L, "bd_heat_slab_advance", [P, C.c_int64])
+    _sig(L, "bd_heat_slab_halo_bytes", [P, C.POINTER(C.c_size_t)])
+    _sig(L, "bd_heat_slab_halo_copy", [P, C.c_int32, C.c_int32, P, P])
+    _sig(L, "bd_heat_slab_finish", [P, P])
+    _sig(L, "bd_heat_slab_end", [P])
     _sig(L, "bd_gilmore_combo_tones", [C.c_double, P, P, P])
     _sig(L, "bd_gilmore_combos", [C.c_int32, C.c_double, C.c_double, P, C.c_int64, C.POINTER(C.c_int64)])
     _sig(L, "bd_gilmore_run", [P, P, C.c_int64, P, P, P, C.POINTER(C.c_double)])
@@ -334,6 +341,11 @@ class Context:
         res["steps_done"] = out.steps_done
         return res
 
+    def heat_slab(self, thermal, Q, traj, z_begin, z_end, max_steps=0):
+        """One rank's z slab of the heat run over the planes [z_begin, z_end)
+        (bd_heat_slab_begin)."""
+        return HeatSlab(self, thermal, Q, traj, z_begin, z_end, max_steps)
+
     # ------------------------------------------------------------ Gilmore
     def gilmore(self, medium, bubbles, ode):
         """bubbles: numpy array of BUBBLE_DTYPE; returns (results RESULT_DTYPE, device ms)."""
@@ -355,6 +367,64 @@ class Context:
         check(self.L.bd_gilmore_threshold_search(self.h, C.byref(medium), _ptr(fr), nc, _ptr(R0), R0.size, ref_arith,
                                                  max_steps, search, _ptr(out), C.byref(ms)))
         return out.reshape(nc, R0.size), ms.value
+
+
+class HeatSlab:
+    """bd_heat_slab_begin / advance / halo_copy / finish / end: one z slab of a
+    heat run, stepped by its caller, who refreshes the ghost plane beyond
+    each internal face between steps."""
+
+    def __init__(self, ctx, thermal, Q, traj, z_begin, z_end, max_steps=0):
+        self.L = ctx.L
+        self.shape = (thermal.nz, thermal.ny, thermal.nx)
+        self.z = (int(z_begin), int(z_end))
+        Q = np.ascontiguousarray(Q, dtype=np.float64).reshape(-1)
+        assert Q.size == thermal.nx * thermal.ny * thermal.nz
+        h = P()
+        check(self.L.bd_heat_slab_begin(ctx.h, C.byref(thermal), _ptr(Q), C.byref(traj), int(max_steps), self.z[0],
+                                        self.z[1], C.byref(h)))
+        self.h = h
+
+    def steps(self):
+        """(steps of the whole run, steps done)"""
+        t, d = C.c_int64(0), C.c_int64(0)
+        check(self.L.bd_heat_slab_steps(self.h, C.byref(t), C.byref(d)))
+        return t.value, d.value
+
+    def advance(self, n):
+        check(self.L.bd_heat_slab_advance(self.h, int(n)))
+
+    def halo_bytes(self):
+        n = C.c_size_t(0)
+        check(self.L.bd_heat_slab_halo_bytes(self.h, C.byref(n)))
+        return n.value
+
+    def halo_copy(self, side, to_ghost, d_ptr, stream=None):
+        check(self.L.bd_heat_slab_halo_copy(self.h, int(side), int(to_ghost), d_ptr, stream))
+
+    def finish(self):
+        """The owned planes of T and the dose, as (z_end - z_begin, ny, nx) arrays."""
+        n = self.shape[0] * self.shape[1] * self.shape[2]
+        T = np.zeros(n, np.float64)
+        D = np.zeros(n, np.float64)
+        out = abi.HeatOutputs()
+        out.T_final = _ptr(T)
+        out.dose = _ptr(D)
+        check(self.L.bd_heat_slab_finish(self.h, C.byref(out)))
+        zb, ze = self.z
+        return {"T": T.reshape(self.shape)[zb:ze].copy(), "dose": D.reshape(self.shape)[zb:ze].copy(),
+                "steps_done": out.steps_done}
+
+    def close(self):
+        if self.h:
+            self.L.bd_heat_slab_end(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class WesterveltSession:

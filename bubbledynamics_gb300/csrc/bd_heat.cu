@@ -15,6 +15,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <memory>
 #include <mutex>
 #include <vector>
 
@@ -271,147 +272,149 @@ static NoallocScratch noalloc_scratch(int dev) {
 
 using namespace bd;
 
-// The heat + dose run (T:345-573) on n_slabs z slabs of this context's device:
-// slab k owns planes [zb_k, ze_k) and keeps one ghost plane beyond each
-// internal face (the 7-point stencil reads iz +- 1, T:72-73), refreshed from
-// the neighbour's newest temperature after every step.  The kernels see each
-// slab as a grid of its local planes, whose first and last planes they never
-// update (the grid's fixed faces, or the ghost planes), so one slab is the
-// whole-grid run and more slabs give its bits.
-static void heat_run(bd_context* ctx, const bd_thermal* th, const double* Q, const bd_trajectory* traj,
-                     int64_t max_steps, int n_slabs, bd_heat_outputs* out) {
-    ctx_check(ctx);
-    if (!th || !Q || !traj || !out) fail(BD_ERR_INVALID_ARG, "null argument");
-    const int nx = th->nx, ny = th->ny, nz = th->nz;
-    if (nx < 3 || ny < 3 || nz < 3) fail(BD_ERR_INVALID_ARG, "grid too small");
-    if (th->n_materials < 1 || th->n_materials > BD_MAX_MATERIALS) fail(BD_ERR_INVALID_ARG, "n_materials out of range");
-    if (th->precision != BD_F32 && th->precision != BD_F64) fail(BD_ERR_INVALID_ARG, "bad precision");
-    const bool f64 = th->precision == BD_F64;
-    const long long plane = (long long)nx * ny, n = plane * nz;
-    // trajectory
+// The heat + dose run (T:345-573) on z slabs: local slab k owns planes
+// [zb_k, ze_k) and keeps one ghost plane beyond each internal face of the grid
+// (the 7-point stencil reads iz +- 1, T:72-73).  The kernels see each slab as a
+// grid of its local planes, whose first and last planes they never update (the
+// grid's fixed faces, or the ghost planes), so one slab is the whole-grid run.
+// Neighbouring local slabs refresh each other's ghost planes after every step;
+// a rank-level slab (bd_heat_slab_*) leaves that to its caller.
+struct HeatSlab {
+    int zb = 0, ze = 0, lo = 0, hi = 0, nzl = 0, zbk = 32;
+    long long nl = 0;                              // local cells
+    PoolBuf Ta, Tb, Qd, TDd;
+    dim3 grid, grid4;
+};
+
+struct HeatPlan {
+    bd_context* ctx = nullptr;
+    bool f64 = false, vec4 = false, use_graph = true, has_pm = false, has_mm = false;
+    int nx = 0, ny = 0, nz = 0, n_legs = 0;
+    long long plane = 0, n = 0;
+    size_t esz = 4;
+    double T_ref = 0.0, dt = 0.0;
     int64_t nsteps = 0;
-    const int leg_cap = 4096;
-    std::vector<int64_t> leg_end(leg_cap, 0);
-    bd_status st = bd_trajectory_shifts(traj, nullptr, nullptr, 0, &nsteps, nullptr, 0);
-    if (st != BD_OK) throw Error{st};
-    std::vector<int32_t> sx(nsteps), sy(nsteps);
-    st = bd_trajectory_shifts(traj, sx.data(), sy.data(), nsteps, &nsteps, leg_end.data(), leg_cap);
-    if (st != BD_OK) throw Error{st};
-    const int n_legs = traj->kind == BD_TRAJ_SPOTS ? traj->n_spots : traj->n_legs;
-    if (max_steps > 0 && max_steps < nsteps) nsteps = max_steps;
-    std::vector<int2> sh(std::max<int64_t>(nsteps, 1));
-    for (int64_t s = 0; s < nsteps; ++s) sh[s] = make_int2(sx[s], sy[s]);
-    if (n_slabs < 1 || n_slabs > nz / 2) fail(BD_ERR_INVALID_ARG, "n_slabs must be in [1, nz / 2]");
-    // initial fields (T:232-257)
-    auto mat_of = [&](long long i) -> int {
-        int iz = (int)(i / plane);
-        int m = th->material_map ? th->material_map[i] : (th->plane_material ? th->plane_material[iz] : 0);
-        if (m < 0 || m >= th->n_materials) fail(BD_ERR_INVALID_ARG, "material index out of range");
-        return m;
-    };
-    const double T_ref = f64 ? 0.0 : th->T_ref;
-    std::vector<double> T0(n), TD0(n);
-    for (long long i = 0; i < n; ++i) {
-        const bd_thermal_material& mt = th->mat[mat_of(i)];
-        T0[i] = th->T_start ? th->T_start[i] : mt.T_init;
-        TD0[i] = th->dose_start ? th->dose_start[i]
-                                : (th->dose_init ? std::pow(4.0, mt.T_init - 273.15 - 43.0) * th->dt : 0.0);   // T:246, T:252
-    }
-    const size_t esz = f64 ? 8 : 4;
-    // slabs: owned planes [zb, ze), local planes [lo, hi) with one ghost plane per internal face
-    struct Slab {
-        int zb, ze, lo, hi, nzl, zbk;
-        long long nl;                                  // local cells
-        PoolBuf Ta, Tb, Qd, TDd;
-        dim3 grid, grid4;
-    };
-    std::vector<Slab> sl(n_slabs);
-    for (int k = 0; k < n_slabs; ++k) {
-        Slab& S = sl[k];
-        S.zb = (int)((long long)nz * k / n_slabs);
-        S.ze = (int)((long long)nz * (k + 1) / n_slabs);
-        S.lo = k > 0 ? S.zb - 1 : 0;
-        S.hi = k + 1 < n_slabs ? S.ze + 1 : nz;
-        S.nzl = S.hi - S.lo;
-        S.nl = plane * S.nzl;
-    }
+    int64_t step = 0;                              // steps done
+    static constexpr int leg_cap = 4096;
+    std::vector<int64_t> leg_end;
     PoolBuf pm, mm, shd, sb;
-    shd.alloc(ctx, sh.size() * sizeof(int2));
-    sb.alloc(ctx, 64);
-    BD_CUDA(cudaMemcpy(shd.p, sh.data(), sh.size() * sizeof(int2), cudaMemcpyHostToDevice));
-    for (Slab& S : sl) {
-        S.Ta.alloc(ctx, S.nl * esz); S.Tb.alloc(ctx, S.nl * esz); S.Qd.alloc(ctx, S.nl * esz);
-        S.TDd.alloc(ctx, S.nl * 8);
-        const long long o = plane * S.lo;
-        if (f64) {
-            BD_CUDA(cudaMemcpy(S.Ta.p, T0.data() + o, S.nl * 8, cudaMemcpyHostToDevice));
-            BD_CUDA(cudaMemcpy(S.Tb.p, T0.data() + o, S.nl * 8, cudaMemcpyHostToDevice));
-            BD_CUDA(cudaMemcpy(S.Qd.p, Q + o, S.nl * 8, cudaMemcpyHostToDevice));
-        } else {
-            std::vector<float> tf(S.nl), qf(S.nl);
-            for (long long i = 0; i < S.nl; ++i) {
-                tf[i] = (float)(T0[o + i] - T_ref);
-                qf[i] = (float)Q[o + i];
-            }
-            BD_CUDA(cudaMemcpy(S.Ta.p, tf.data(), S.nl * 4, cudaMemcpyHostToDevice));
-            BD_CUDA(cudaMemcpy(S.Tb.p, tf.data(), S.nl * 4, cudaMemcpyHostToDevice));
-            BD_CUDA(cudaMemcpy(S.Qd.p, qf.data(), S.nl * 4, cudaMemcpyHostToDevice));
+    std::vector<HeatSlab> sl;
+    HeatArgs<float> af{};
+    HeatArgs<double> ad{};
+    static constexpr int CH = 64;
+    cudaGraphExec_t graphs[2] = {nullptr, nullptr};
+    ~HeatPlan() {
+        for (auto e : graphs)
+            if (e) cudaGraphExecDestroy(e);
+    }
+
+    // checks, trajectory, initial fields (T:232-257) and the device buffers of
+    // the slabs owning the given plane ranges
+    void prepare(bd_context* c, const bd_thermal* th, const double* Q, const bd_trajectory* traj, int64_t max_steps,
+                 const std::vector<std::pair<int, int>>& owned) {
+        ctx = c;
+        ctx_check(ctx);
+        if (!th || !Q || !traj) fail(BD_ERR_INVALID_ARG, "null argument");
+        nx = th->nx; ny = th->ny; nz = th->nz;
+        if (nx < 3 || ny < 3 || nz < 3) fail(BD_ERR_INVALID_ARG, "grid too small");
+        if (th->n_materials < 1 || th->n_materials > BD_MAX_MATERIALS)
+            fail(BD_ERR_INVALID_ARG, "n_materials out of range");
+        if (th->precision != BD_F32 && th->precision != BD_F64) fail(BD_ERR_INVALID_ARG, "bad precision");
+        for (size_t k = 0; k < owned.size(); ++k) {
+            const int zb = owned[k].first, ze = owned[k].second;
+            if (!(0 <= zb && zb + 2 <= ze && ze <= nz)) fail(BD_ERR_INVALID_ARG, "slab [%d, %d) of %d planes", zb, ze, nz);
+            if (k > 0 && owned[k - 1].second != zb) fail(BD_ERR_INVALID_ARG, "local slabs must be contiguous");
         }
-        BD_CUDA(cudaMemcpy(S.TDd.p, TD0.data() + o, S.nl * 8, cudaMemcpyHostToDevice));
-    }
-    if (th->plane_material) {
-        pm.alloc(ctx, nz * 4);
-        BD_CUDA(cudaMemcpy(pm.p, th->plane_material, nz * 4, cudaMemcpyHostToDevice));
-    }
-    if (th->material_map) {
-        mm.alloc(ctx, n);
-        BD_CUDA(cudaMemcpy(mm.p, th->material_map, n, cudaMemcpyHostToDevice));
-    }
-    BD_CUDA(cudaMemset(sb.p, 0, 64));
-    cudaStream_t s = ctx->stream;
-    const bool vec4 = !f64 && nx % 4 == 0;
-    static int per_sm4 = 0;
-    if (vec4 && !per_sm4) BD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm4, heat_step4_kernel, 128, 0));
-    for (Slab& S : sl) {
-        S.zbk = 32;
-        if (vec4) {
-            // four-cell kernel: z-chunk fitted to whole waves of its resident CTAs
-            const long long tiles = (long long)((nx / 4 + 15) / 16) * ((ny + 7) / 8);
-            S.zbk = wave_fitted_zb(tiles, S.nzl, (long long)ctx->sm_count * std::max(per_sm4, 1), 0.9);
+        f64 = th->precision == BD_F64;
+        plane = (long long)nx * ny;
+        n = plane * nz;
+        dt = th->dt;
+        use_graph = th->plain_launches == 0;
+        // trajectory
+        leg_end.assign(leg_cap, 0);
+        bd_status st = bd_trajectory_shifts(traj, nullptr, nullptr, 0, &nsteps, nullptr, 0);
+        if (st != BD_OK) throw Error{st};
+        std::vector<int32_t> sx(nsteps), sy(nsteps);
+        st = bd_trajectory_shifts(traj, sx.data(), sy.data(), nsteps, &nsteps, leg_end.data(), leg_cap);
+        if (st != BD_OK) throw Error{st};
+        n_legs = traj->kind == BD_TRAJ_SPOTS ? traj->n_spots : traj->n_legs;
+        if (max_steps > 0 && max_steps < nsteps) nsteps = max_steps;
+        std::vector<int2> sh(std::max<int64_t>(nsteps, 1));
+        for (int64_t s = 0; s < nsteps; ++s) sh[s] = make_int2(sx[s], sy[s]);
+        // initial fields (T:232-257)
+        auto mat_of = [&](long long i) -> int {
+            int iz = (int)(i / plane);
+            int m = th->material_map ? th->material_map[i] : (th->plane_material ? th->plane_material[iz] : 0);
+            if (m < 0 || m >= th->n_materials) fail(BD_ERR_INVALID_ARG, "material index out of range");
+            return m;
+        };
+        T_ref = f64 ? 0.0 : th->T_ref;
+        std::vector<double> T0(n), TD0(n);
+        for (long long i = 0; i < n; ++i) {
+            const bd_thermal_material& mt = th->mat[mat_of(i)];
+            T0[i] = th->T_start ? th->T_start[i] : mt.T_init;
+            TD0[i] = th->dose_start ? th->dose_start[i]
+                                    : (th->dose_init ? std::pow(4.0, mt.T_init - 273.15 - 43.0) * th->dt : 0.0);   // T:246, T:252
         }
-        S.grid = dim3((nx + 31) / 32, (ny + 7) / 8, (S.nzl + S.zbk - 1) / S.zbk);
-        S.grid4 = dim3((nx / 4 + 15) / 16, (ny + 7) / 8, (S.nzl + S.zbk - 1) / S.zbk);
-    }
-    const dim3 block(32, 8), block4(16, 8);
-    // snapshot schedule: after the listed legs (T:412-563)
-    std::vector<std::pair<int64_t, int>> snaps;
-    for (int k = 0; k < out->n_snap; ++k) {
-        const int leg = out->snapshot_legs ? out->snapshot_legs[k] : 0;
-        if (leg < 1 || leg > n_legs || leg > leg_cap) fail(BD_ERR_INVALID_ARG, "snapshot leg %d out of range", leg);
-        snaps.push_back({leg_end[leg - 1], k});
-    }
-    std::sort(snaps.begin(), snaps.end());
-    // the owned planes of every slab's temperature after `steps` steps, as T in the whole grid
-    auto copy_T = [&](int64_t steps, double* dst) {
-        for (const Slab& S : sl) {
-            const PoolBuf& src = (steps % 2 == 0) ? S.Ta : S.Tb;
-            const long long off = plane * (S.zb - S.lo), cnt = plane * (S.ze - S.zb);
-            double* d = dst + plane * S.zb;
+        esz = f64 ? 8 : 4;
+        std::vector<HeatSlab>(owned.size()).swap(sl);
+        for (size_t k = 0; k < owned.size(); ++k) {
+            HeatSlab& S = sl[k];
+            S.zb = owned[k].first;
+            S.ze = owned[k].second;
+            S.lo = S.zb > 0 ? S.zb - 1 : 0;
+            S.hi = S.ze < nz ? S.ze + 1 : nz;
+            S.nzl = S.hi - S.lo;
+            S.nl = plane * S.nzl;
+        }
+        shd.alloc(ctx, sh.size() * sizeof(int2));
+        sb.alloc(ctx, 64);
+        BD_CUDA(cudaMemcpy(shd.p, sh.data(), sh.size() * sizeof(int2), cudaMemcpyHostToDevice));
+        for (HeatSlab& S : sl) {
+            S.Ta.alloc(ctx, S.nl * esz); S.Tb.alloc(ctx, S.nl * esz); S.Qd.alloc(ctx, S.nl * esz);
+            S.TDd.alloc(ctx, S.nl * 8);
+            const long long o = plane * S.lo;
             if (f64) {
-                BD_CUDA(cudaMemcpyAsync(d, static_cast<const double*>(src.p) + off, cnt * 8, cudaMemcpyDeviceToHost, s));
-                BD_CUDA(cudaStreamSynchronize(s));
+                BD_CUDA(cudaMemcpy(S.Ta.p, T0.data() + o, S.nl * 8, cudaMemcpyHostToDevice));
+                BD_CUDA(cudaMemcpy(S.Tb.p, T0.data() + o, S.nl * 8, cudaMemcpyHostToDevice));
+                BD_CUDA(cudaMemcpy(S.Qd.p, Q + o, S.nl * 8, cudaMemcpyHostToDevice));
             } else {
-                std::vector<float> tf(cnt);
-                BD_CUDA(cudaMemcpyAsync(tf.data(), static_cast<const float*>(src.p) + off, cnt * 4,
-                                        cudaMemcpyDeviceToHost, s));
-                BD_CUDA(cudaStreamSynchronize(s));
-                for (long long i = 0; i < cnt; ++i) d[i] = T_ref + (double)tf[i];
+                std::vector<float> tf(S.nl), qf(S.nl);
+                for (long long i = 0; i < S.nl; ++i) {
+                    tf[i] = (float)(T0[o + i] - T_ref);
+                    qf[i] = (float)Q[o + i];
+                }
+                BD_CUDA(cudaMemcpy(S.Ta.p, tf.data(), S.nl * 4, cudaMemcpyHostToDevice));
+                BD_CUDA(cudaMemcpy(S.Tb.p, tf.data(), S.nl * 4, cudaMemcpyHostToDevice));
+                BD_CUDA(cudaMemcpy(S.Qd.p, qf.data(), S.nl * 4, cudaMemcpyHostToDevice));
             }
+            BD_CUDA(cudaMemcpy(S.TDd.p, TD0.data() + o, S.nl * 8, cudaMemcpyHostToDevice));
         }
-    };
-    auto make_args = [&]() {
-        HeatArgs<float> af;
-        HeatArgs<double> ad;
+        has_pm = th->plane_material != nullptr;
+        has_mm = th->material_map != nullptr;
+        if (has_pm) {
+            pm.alloc(ctx, nz * 4);
+            BD_CUDA(cudaMemcpy(pm.p, th->plane_material, nz * 4, cudaMemcpyHostToDevice));
+        }
+        if (has_mm) {
+            mm.alloc(ctx, n);
+            BD_CUDA(cudaMemcpy(mm.p, th->material_map, n, cudaMemcpyHostToDevice));
+        }
+        BD_CUDA(cudaMemset(sb.p, 0, 64));
+        vec4 = !f64 && nx % 4 == 0;
+        static int per_sm4 = 0;
+        if (vec4 && !per_sm4) BD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm4, heat_step4_kernel, 128, 0));
+        for (HeatSlab& S : sl) {
+            S.zbk = 32;
+            if (vec4) {
+                // four-cell kernel: z-chunk fitted to whole waves of its resident CTAs
+                const long long tiles = (long long)((nx / 4 + 15) / 16) * ((ny + 7) / 8);
+                S.zbk = wave_fitted_zb(tiles, S.nzl, (long long)ctx->sm_count * std::max(per_sm4, 1), 0.9);
+            }
+            S.grid = dim3((nx + 31) / 32, (ny + 7) / 8, (S.nzl + S.zbk - 1) / S.zbk);
+            S.grid4 = dim3((nx / 4 + 15) / 16, (ny + 7) / 8, (S.nzl + S.zbk - 1) / S.zbk);
+        }
+        // material constants (T:212-217, plus the Pennes term)
         std::memset(&af, 0, sizeof af);
         std::memset(&ad, 0, sizeof ad);
         for (int k = 0; k < th->n_materials; ++k) {
@@ -425,57 +428,60 @@ static void heat_run(bd_context* ctx, const bd_thermal* th, const double* Q, con
             af.mat[k] = HeatMat<float>{(float)a0, (float)kxy, (float)kz, (float)qc, (float)wTa};
             ad.mat[k] = HeatMat<double>{a0, kxy, kz, qc, wTa};
         }
-        return std::make_pair(af, ad);
-    };
-    auto margs = make_args();
-    auto fill = [&](auto& a, const Slab& S, bool a_to_b, auto tag) {
-        using RR = decltype(tag);
+        step = 0;
+    }
+
+    template <class A, class RR>
+    void fill(A& a, const HeatSlab& S, bool a_to_b) const {
         a.nx = nx; a.ny = ny; a.nz = S.nzl; a.zb = S.zbk; a.plane = plane;
         a.Tin = (a_to_b ? S.Ta : S.Tb).template as<RR>();
         a.Tout = (a_to_b ? S.Tb : S.Ta).template as<RR>();
         a.Q = S.Qd.template as<RR>();
         a.TD = S.TDd.template as<double>();
         a.TDf = nullptr;
-        a.plane_mat = th->plane_material ? pm.template as<int>() + S.lo : nullptr;
-        a.matmap = th->material_map ? mm.template as<uint8_t>() + plane * S.lo : nullptr;
+        a.plane_mat = has_pm ? pm.template as<int>() + S.lo : nullptr;
+        a.matmap = has_mm ? mm.template as<uint8_t>() + plane * S.lo : nullptr;
         a.shifts = shd.template as<int2>();
         a.step_base = sb.template as<long long>();
-        a.dt = (RR)th->dt;
+        a.dt = (RR)dt;
         a.T_ref = T_ref;
         a.T_refm43 = (float)(T_ref - 273.15 - 43.0);
-    };
-    // after a step, the ghost planes of its output take the neighbours' newest owned planes
-    auto exchange = [&](cudaStream_t st, bool a_to_b) {
-        for (int k = 0; k + 1 < n_slabs; ++k) {
-            const Slab& L = sl[k];
-            const Slab& U = sl[k + 1];
+    }
+
+    // the newest temperature of a slab after `steps` steps (the reference
+    // toggles use_p each step, T:391; with Tin/Tout swapped per step the latest
+    // field is Ta after an even number of steps)
+    const PoolBuf& newest(const HeatSlab& S, int64_t steps) const { return (steps % 2 == 0) ? S.Ta : S.Tb; }
+
+    // after a step, the ghost planes of neighbouring local slabs take each other's newest owned planes
+    void exchange(cudaStream_t st, bool a_to_b) {
+        const size_t pb = (size_t)plane * esz;
+        for (size_t k = 0; k + 1 < sl.size(); ++k) {
+            const HeatSlab& L = sl[k];
+            const HeatSlab& U = sl[k + 1];
             unsigned char* lo_f = static_cast<unsigned char*>((a_to_b ? L.Tb : L.Ta).p);
             unsigned char* up_f = static_cast<unsigned char*>((a_to_b ? U.Tb : U.Ta).p);
-            const size_t pb = (size_t)plane * esz;
             // L's last owned plane -> U's lower ghost; U's first owned plane -> L's upper ghost
             BD_CUDA(cudaMemcpyAsync(up_f, lo_f + (size_t)(L.ze - 1 - L.lo) * pb, pb, cudaMemcpyDeviceToDevice, st));
             BD_CUDA(cudaMemcpyAsync(lo_f + (size_t)(L.hi - 1 - L.lo) * pb, up_f + (size_t)(U.zb - U.lo) * pb, pb,
                                     cudaMemcpyDeviceToDevice, st));
         }
-    };
-    // the reference toggles use_p each step (T:391); with Tin/Tout swapped per
-    // step, after an even number of steps the latest field is Ta.  Steps go
-    // out in chunks of CH: the kernels read their step as the device counter
-    // plus their offset in the chunk, and one advance kernel moves the counter,
-    // so a chunk depends only on the parity of its first step and one captured
-    // CUDA graph per parity serves every full chunk.
-    const int CH = 64;
-    auto issue = [&](cudaStream_t st, int64_t s0, int cnt) {
+    }
+
+    // steps s0 .. s0 + cnt - 1 of every local slab: the kernels read their step as
+    // the device counter plus their offset, and one advance kernel moves the counter
+    void issue(cudaStream_t st, int64_t s0, int cnt) {
+        const dim3 block(32, 8), block4(16, 8);
         for (int k = 0; k < cnt; ++k) {
             const bool a_to_b = ((s0 + k) % 2) == 0;
-            for (const Slab& S : sl) {
+            for (const HeatSlab& S : sl) {
                 if (f64) {
-                    HeatArgs<double> a = margs.second;
-                    fill(a, S, a_to_b, 0.0);
+                    HeatArgs<double> a = ad;
+                    fill<HeatArgs<double>, double>(a, S, a_to_b);
                     heat_step_kernel<double><<<S.grid, block, 0, st>>>(a, k);
                 } else {
-                    HeatArgs<float> a = margs.first;
-                    fill(a, S, a_to_b, 0.0f);
+                    HeatArgs<float> a = af;
+                    fill<HeatArgs<float>, float>(a, S, a_to_b);
                     if (vec4) heat_step4_kernel<<<S.grid4, block4, 0, st>>>(a, k);
                     else heat_step_kernel<float><<<S.grid, block, 0, st>>>(a, k);
                 }
@@ -485,13 +491,12 @@ static void heat_run(bd_context* ctx, const bd_thermal* th, const double* Q, con
         }
         heat_advance_kernel<<<1, 32, 0, st>>>(sb.as<long long>(), cnt);
         BD_LAUNCHED(ctx);
-    };
-    struct Graphs {
-        cudaGraphExec_t g[2] = {nullptr, nullptr};
-        ~Graphs() { for (auto e : g) if (e) cudaGraphExecDestroy(e); }
-    } graphs;
-    auto chunk_graph = [&](int parity) {
-        if (graphs.g[parity]) return graphs.g[parity];
+    }
+
+    // a chunk depends only on the parity of its first step, so one captured
+    // CUDA graph per parity serves every full chunk of CH steps
+    cudaGraphExec_t chunk_graph(int parity) {
+        if (graphs[parity]) return graphs[parity];
         cudaStream_t cs;
         BD_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
         cudaGraph_t g = nullptr;
@@ -507,53 +512,102 @@ static void heat_run(bd_context* ctx, const bd_thermal* th, const double* Q, con
         }
         BD_CUDA(cudaStreamEndCapture(cs, &g));
         ctx->launches = before;   // captured, not launched
-        const cudaError_t e = cudaGraphInstantiate(&graphs.g[parity], g, 0);
+        const cudaError_t e = cudaGraphInstantiate(&graphs[parity], g, 0);
         cudaGraphDestroy(g);
         cudaStreamDestroy(cs);
         BD_CUDA(e);
-        return graphs.g[parity];
-    };
-    const bool use_graph = th->plain_launches == 0;
-    BD_CUDA(cudaEventRecord(ctx->ev0, s));
-    int64_t done = 0;
-    size_t isnap = 0;
-    auto run_steps = [&](int64_t from, int64_t to) {
+        return graphs[parity];
+    }
+
+    void run_steps(int64_t from, int64_t to) {
         for (int64_t s0 = from; s0 < to; s0 += CH) {
             const int cnt = (int)std::min<int64_t>(CH, to - s0);
             if (use_graph && cnt == CH) {
-                BD_CUDA(cudaGraphLaunch(chunk_graph((int)(s0 % 2)), s));
-                ctx->launches += (int64_t)CH * n_slabs + 1;
+                BD_CUDA(cudaGraphLaunch(chunk_graph((int)(s0 % 2)), ctx->stream));
+                ctx->launches += (int64_t)CH * sl.size() + 1;
             } else {
-                issue(s, s0, cnt);
+                issue(ctx->stream, s0, cnt);
             }
         }
-    };
+        step = to;
+    }
+
+    // the owned planes of every local slab's temperature after `steps` steps, into the whole grid's T
+    void copy_T(int64_t steps, double* dst) {
+        cudaStream_t s = ctx->stream;
+        for (const HeatSlab& S : sl) {
+            const PoolBuf& src = newest(S, steps);
+            const long long off = plane * (S.zb - S.lo), cnt = plane * (S.ze - S.zb);
+            double* d = dst + plane * S.zb;
+            if (f64) {
+                BD_CUDA(cudaMemcpyAsync(d, static_cast<const double*>(src.p) + off, cnt * 8, cudaMemcpyDeviceToHost, s));
+                BD_CUDA(cudaStreamSynchronize(s));
+            } else {
+                std::vector<float> tf(cnt);
+                BD_CUDA(cudaMemcpyAsync(tf.data(), static_cast<const float*>(src.p) + off, cnt * 4,
+                                        cudaMemcpyDeviceToHost, s));
+                BD_CUDA(cudaStreamSynchronize(s));
+                for (long long i = 0; i < cnt; ++i) d[i] = T_ref + (double)tf[i];
+            }
+        }
+    }
+
+    void copy_dose(double* dst) {
+        for (const HeatSlab& S : sl)
+            BD_CUDA(cudaMemcpy(dst + plane * S.zb, static_cast<const double*>(S.TDd.p) + plane * (S.zb - S.lo),
+                               (size_t)plane * (S.ze - S.zb) * 8, cudaMemcpyDeviceToHost));
+    }
+};
+
+static void heat_run(bd_context* ctx, const bd_thermal* th, const double* Q, const bd_trajectory* traj,
+                     int64_t max_steps, int n_slabs, bd_heat_outputs* out) {
+    ctx_check(ctx);
+    if (!th || !out) fail(BD_ERR_INVALID_ARG, "null argument");
+    if (n_slabs < 1 || n_slabs > th->nz / 2) fail(BD_ERR_INVALID_ARG, "n_slabs must be in [1, nz / 2]");
+    std::vector<std::pair<int, int>> owned;
+    for (int k = 0; k < n_slabs; ++k)
+        owned.push_back({(int)((long long)th->nz * k / n_slabs), (int)((long long)th->nz * (k + 1) / n_slabs)});
+    HeatPlan P;
+    P.prepare(ctx, th, Q, traj, max_steps, owned);
+    // snapshot schedule: after the listed legs (T:412-563)
+    std::vector<std::pair<int64_t, int>> snaps;
+    for (int k = 0; k < out->n_snap; ++k) {
+        const int leg = out->snapshot_legs ? out->snapshot_legs[k] : 0;
+        if (leg < 1 || leg > P.n_legs || leg > HeatPlan::leg_cap) fail(BD_ERR_INVALID_ARG, "snapshot leg %d out of range", leg);
+        snaps.push_back({P.leg_end[leg - 1], k});
+    }
+    std::sort(snaps.begin(), snaps.end());
+    cudaStream_t s = ctx->stream;
+    BD_CUDA(cudaEventRecord(ctx->ev0, s));
+    int64_t done = 0;
+    size_t isnap = 0;
     while (true) {
         // snapshots due at this step (a leg of zero steps ends where it starts)
         while (isnap < snaps.size() && snaps[isnap].first <= done) {
             if (out->snapshots)
-                copy_T(done, static_cast<double*>(out->snapshots) + (size_t)snaps[isnap].second * n);
+                P.copy_T(done, static_cast<double*>(out->snapshots) + (size_t)snaps[isnap].second * P.n);
             ++isnap;
         }
-        if (done >= nsteps) break;
-        int64_t next = nsteps;
+        if (done >= P.nsteps) break;
+        int64_t next = P.nsteps;
         if (isnap < snaps.size()) next = std::min<int64_t>(next, snaps[isnap].first);
-        run_steps(done, next);
+        P.run_steps(done, next);
         done = next;
     }
     BD_CUDA(cudaEventRecord(ctx->ev1, s));
     BD_CUDA(cudaEventSynchronize(ctx->ev1));
     float ms = 0;
     BD_CUDA(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
-    if (out->T_final) copy_T(nsteps, static_cast<double*>(out->T_final));
-    if (out->dose)
-        for (const Slab& S : sl)
-            BD_CUDA(cudaMemcpy(static_cast<double*>(out->dose) + plane * S.zb,
-                               static_cast<const double*>(S.TDd.p) + plane * (S.zb - S.lo),
-                               (size_t)plane * (S.ze - S.zb) * 8, cudaMemcpyDeviceToHost));
+    if (out->T_final) P.copy_T(P.nsteps, static_cast<double*>(out->T_final));
+    if (out->dose) P.copy_dose(static_cast<double*>(out->dose));
     out->elapsed_ms = ms;
-    out->steps_done = nsteps;
+    out->steps_done = P.nsteps;
 }
+
+// One rank's z slab of a heat run (bd_heat_slab_begin .. _end).
+struct bd_heat_slab {
+    HeatPlan P;
+};
 
 extern "C" {
 
@@ -631,6 +685,76 @@ bd_status bd_spiral_heat_run(bd_context* ctx, const bd_thermal* th, const double
 bd_status bd_spiral_heat_run_slabs(bd_context* ctx, const bd_thermal* th, const double* Q, const bd_trajectory* traj,
                                    int64_t max_steps, int32_t n_slabs, bd_heat_outputs* out) {
     return guard([&] { heat_run(ctx, th, Q, traj, max_steps, n_slabs, out); });
+}
+
+bd_status bd_heat_slab_begin(bd_context* ctx, const bd_thermal* th, const double* Q, const bd_trajectory* traj,
+                             int64_t max_steps, int32_t z_begin, int32_t z_end, bd_heat_slab** out) {
+    return guard([&] {
+        if (!out) fail(BD_ERR_INVALID_ARG, "null output");
+        *out = nullptr;
+        std::unique_ptr<bd_heat_slab> h(new bd_heat_slab());
+        h->P.prepare(ctx, th, Q, traj, max_steps, {{z_begin, z_end}});
+        h->P.use_graph = false;                  // one step at a time between halo refreshes
+        *out = h.release();
+    });
+}
+
+bd_status bd_heat_slab_steps(bd_heat_slab* h, int64_t* total, int64_t* done) {
+    return guard([&] {
+        if (!h) fail(BD_ERR_INVALID_ARG, "null slab");
+        if (total) *total = h->P.nsteps;
+        if (done) *done = h->P.step;
+    });
+}
+
+bd_status bd_heat_slab_advance(bd_heat_slab* h, int64_t n) {
+    return guard([&] {
+        if (!h) fail(BD_ERR_INVALID_ARG, "null slab");
+        ctx_check(h->P.ctx);
+        if (n < 0 || h->P.step + n > h->P.nsteps) fail(BD_ERR_INVALID_ARG, "advance past the end of the run");
+        h->P.run_steps(h->P.step, h->P.step + n);
+        BD_CUDA(cudaStreamSynchronize(h->P.ctx->stream));   // the steps are done when this returns
+    });
+}
+
+bd_status bd_heat_slab_halo_bytes(bd_heat_slab* h, size_t* bytes) {
+    return guard([&] {
+        if (!h || !bytes) fail(BD_ERR_INVALID_ARG, "null argument");
+        *bytes = (size_t)h->P.plane * h->P.esz;
+    });
+}
+
+bd_status bd_heat_slab_halo_copy(bd_heat_slab* h, int32_t side, int32_t to_ghost, void* d_buf, void* stream) {
+    return guard([&] {
+        if (!h || !d_buf) fail(BD_ERR_INVALID_ARG, "null argument");
+        ctx_check(h->P.ctx);
+        const HeatSlab& S = h->P.sl[0];
+        if (side != 0 && side != 1) fail(BD_ERR_INVALID_ARG, "side must be 0 or 1");
+        if ((side == 0 && S.zb == 0) || (side == 1 && S.ze == h->P.nz))
+            fail(BD_ERR_INVALID_ARG, "side %d of this slab is a face of the grid", side);
+        const size_t pb = (size_t)h->P.plane * h->P.esz;
+        // the newest temperature: the owned plane next to the face, or the ghost plane beyond it
+        const int local = side == 0 ? (to_ghost ? 0 : 1) : (to_ghost ? S.nzl - 1 : S.nzl - 2);
+        char* plane = static_cast<char*>(h->P.newest(S, h->P.step).p) + (size_t)local * pb;
+        cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : h->P.ctx->stream;
+        if (to_ghost) BD_CUDA(cudaMemcpyAsync(plane, d_buf, pb, cudaMemcpyDeviceToDevice, st));
+        else BD_CUDA(cudaMemcpyAsync(d_buf, plane, pb, cudaMemcpyDeviceToDevice, st));
+    });
+}
+
+bd_status bd_heat_slab_finish(bd_heat_slab* h, bd_heat_outputs* out) {
+    return guard([&] {
+        if (!h || !out) fail(BD_ERR_INVALID_ARG, "null argument");
+        ctx_check(h->P.ctx);
+        BD_CUDA(cudaStreamSynchronize(h->P.ctx->stream));
+        if (out->T_final) h->P.copy_T(h->P.step, static_cast<double*>(out->T_final));
+        if (out->dose) h->P.copy_dose(static_cast<double*>(out->dose));
+        out->steps_done = h->P.step;
+    });
+}
+
+bd_status bd_heat_slab_end(bd_heat_slab* h) {
+    return guard([&] { delete h; });
 }
 
 bd_status bd_heat_run_device_noalloc(bd_context* ctx, const bd_thermal* th, float* d_theta, const float* d_Q,

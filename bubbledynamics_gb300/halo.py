@@ -1,4 +1,4 @@
-"""z-slab decomposition of the Westervelt solve across ranks.
+"""z-slab decomposition of the Westervelt and heat solves across ranks.
 
 The reference runs one grid on one device (W:353).  Here a grid of nz planes
 is split into contiguous slabs of whole planes, one per rank; each rank keeps 3
@@ -15,6 +15,9 @@ the peak, energy and DFT maps are per cell, so nothing else is exchanged.
   time, pack / exchange / unpack through the library's halo copies.
 * `run_slabs_local(ctx, prob, n)` — the same data path for n slabs held by one
   process on one device (the buffers are handed over in place of messages).
+* `run_heat_slab_rank(...)`, `run_heat_slabs_local(...)` — the same for the
+  heat run, whose 7-point stencil reaches one plane (T:72-73): one ghost plane
+  per internal face, slabs of at least 2 planes.
 """
 import numpy as np
 
@@ -113,3 +116,80 @@ def run_slabs_local(ctx, prob, n_slabs, want=("p_final", "peak", "energy", "Q"))
         for s in slabs:
             s.close()
     return {k: np.concatenate([p[k] for p in parts], axis=0) for k in parts[0] if k != "steps_done"}
+
+
+def heat_slab_bounds(nz, n):
+    """[z_begin, z_end) of n heat slabs of nz planes (the split
+    bd_spiral_heat_run_slabs uses; at least 2 planes each)."""
+    if n < 1 or nz < 2 * n:
+        raise ValueError("%d planes cannot make %d slabs of at least 2 planes" % (nz, n))
+    return [(nz * k // n, nz * (k + 1) // n) for k in range(n)]
+
+
+def _heat_refresh(slabs, bufs, stream):
+    """Ghost planes of neighbouring heat slabs of one process through device
+    buffers: pack every slab's boundary planes, then unpack the neighbours'."""
+    n = len(slabs)
+    for k, s in enumerate(slabs):
+        if k > 0:
+            s.halo_copy(0, 0, bufs[k][0].data_ptr(), stream)
+        if k + 1 < n:
+            s.halo_copy(1, 0, bufs[k][1].data_ptr(), stream)
+    for k, s in enumerate(slabs):
+        if k > 0:
+            s.halo_copy(0, 1, bufs[k - 1][1].data_ptr(), stream)     # from the slab below
+        if k + 1 < n:
+            s.halo_copy(1, 1, bufs[k + 1][0].data_ptr(), stream)     # from the slab above
+
+
+def run_heat_slab_rank(ctx, thermal, Q, traj, max_steps=0, group=None):
+    """This rank's slab of the heat run, stepped with a ghost-plane refresh
+    after every step over torch.distributed; returns its owned planes of T and
+    the dose (see HeatSlab.finish)."""
+    import torch
+    import torch.distributed as dist
+    world = dist.get_world_size(group)
+    rank = dist.get_rank(group)
+    zb, ze = heat_slab_bounds(thermal.nz, world)[rank]
+    s = ctx.heat_slab(thermal, Q, traj, zb, ze, max_steps)
+    send_lo, send_hi, recv_lo, recv_hi = _halo_buffers(s, 4)
+    stream = torch.cuda.current_stream().cuda_stream
+    total, _ = s.steps()
+    for _ in range(total):
+        s.advance(1)
+        if rank > 0:
+            s.halo_copy(0, 0, send_lo.data_ptr(), stream)
+        if rank + 1 < world:
+            s.halo_copy(1, 0, send_hi.data_ptr(), stream)
+        exchange_halos(send_lo, send_hi, recv_lo, recv_hi, rank, world, group)
+        if rank > 0:
+            s.halo_copy(0, 1, recv_lo.data_ptr(), stream)
+        if rank + 1 < world:
+            s.halo_copy(1, 1, recv_hi.data_ptr(), stream)
+        torch.cuda.current_stream().synchronize()
+    out = s.finish()
+    s.close()
+    return out
+
+
+def run_heat_slabs_local(ctx, thermal, Q, traj, n_slabs, max_steps=0):
+    """n_slabs heat slabs in this process, stepped in lockstep, the ghost planes
+    travelling through device buffers as run_heat_slab_rank's messages do.
+    Returns the whole grid's T and dose."""
+    import torch
+    bounds = heat_slab_bounds(thermal.nz, n_slabs)
+    slabs = [ctx.heat_slab(thermal, Q, traj, zb, ze, max_steps) for zb, ze in bounds]
+    bufs = [_halo_buffers(s, 2) for s in slabs]      # [k][0]: going down, [k][1]: going up
+    stream = torch.cuda.current_stream().cuda_stream
+    try:
+        total, _ = slabs[0].steps()
+        for _ in range(total):
+            for s in slabs:
+                s.advance(1)
+            _heat_refresh(slabs, bufs, stream)
+            torch.cuda.current_stream().synchronize()
+        parts = [s.finish() for s in slabs]
+    finally:
+        for s in slabs:
+            s.close()
+    return {k: np.concatenate([p[k] for p in parts], axis=0) for k in ("T", "dose")}

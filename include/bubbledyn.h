@@ -404,6 +404,29 @@ bd_status bd_spiral_heat_run_slabs(bd_context* ctx, const bd_thermal* thermal, c
                                    const bd_trajectory* traj, int64_t max_steps, int32_t n_slabs,
                                    bd_heat_outputs* out);
 
+/* One rank's z slab of the heat run (the multi-GPU split of T:345-573; the
+ * reference runs one grid on one device, T:112): the slab owns planes
+ * [z_begin, z_end) (at least 2) of the whole problem and keeps one ghost plane
+ * beyond each internal face.  The caller steps it (bd_heat_slab_advance, which
+ * returns once the steps are done) and refreshes the ghost planes between
+ * steps: bd_heat_slab_halo_copy with to_ghost = 0 copies the newest owned
+ * plane next to face `side` (0 = low z, 1 = high z) into d_buf (one plane,
+ * bd_heat_slab_halo_bytes), to_ghost = 1 copies d_buf into the ghost plane
+ * beyond it; the transport between devices is the caller's.  Enqueued on
+ * stream (NULL = the context's stream).  bd_heat_slab_finish writes the owned
+ * planes of T and the dose into whole-grid host arrays at their own offsets
+ * (T_final / dose of bd_heat_outputs; snapshots are not taken). */
+typedef struct bd_heat_slab bd_heat_slab;
+bd_status bd_heat_slab_begin(bd_context* ctx, const bd_thermal* thermal, const double* Q,
+                             const bd_trajectory* traj, int64_t max_steps, int32_t z_begin, int32_t z_end,
+                             bd_heat_slab** out);
+bd_status bd_heat_slab_steps(bd_heat_slab* slab, int64_t* total, int64_t* done);
+bd_status bd_heat_slab_advance(bd_heat_slab* slab, int64_t n);
+bd_status bd_heat_slab_halo_bytes(bd_heat_slab* slab, size_t* bytes);
+bd_status bd_heat_slab_halo_copy(bd_heat_slab* slab, int32_t side, int32_t to_ghost, void* d_buf, void* stream);
+bd_status bd_heat_slab_finish(bd_heat_slab* slab, bd_heat_outputs* out);
+bd_status bd_heat_slab_end(bd_heat_slab* slab);
+
 /* Allocation-free variant of the FP32 heat + dose run, for callers that
  * cannot call cudaMalloc: code running inside another framework's memory
  * arena, which owns the device memory and forbids driver allocations, or a

@@ -129,3 +129,38 @@ def test_heat_slab_count_checked(ctx):
     k, prob, sx, sy, Q = mini()
     with pytest.raises(api.BDError):
         ctx.heat(prob.thermal, Q, prob.traj, n_slabs=prob.thermal.nz)   # fewer than 2 planes per slab
+
+
+@pytest.mark.parametrize("precision,nxy", [(abi.BD_F32, 44), (abi.BD_F64, 41)])
+def test_heat_slab_sessions_through_halo_buffers(ctx, precision, nxy):
+    """The data path of a multi-rank heat run (each slab its own session,
+    stepped one step at a time; pack the owned boundary plane into a device
+    buffer, hand it over, unpack into the neighbour's ghost plane) for 2 and 3
+    slab sessions in this process: the one-domain T and dose bit for bit."""
+    torch = pytest.importorskip("torch")
+    from bubbledynamics_gb300 import halo
+    k = presets.ref_T_mini_constants(Nxy=nxy, Nz=30, legs=2)
+    Q = presets.gaussian_focus_Q((30, nxy, nxy), (16, 20, 20), (3.0, 2.0, 2.0), 4.0e7)
+
+    def problem():
+        prob = presets.make_ref_T(k, precision=precision)
+        prob.set_spots([0, 4, -3], [0, 2, 5], [41, 30, 29])
+        return prob
+    p = problem()
+    one = ctx.heat(p.thermal, Q, p.traj)
+    assert one["steps_done"] == 100
+    for n_slabs in (2, 3):
+        p = problem()
+        got = halo.run_heat_slabs_local(ctx, p.thermal, Q, p.traj, n_slabs)
+        np.testing.assert_array_equal(got["T"], one["T"], err_msg="T, %d slabs" % n_slabs)
+        np.testing.assert_array_equal(got["dose"], one["dose"], err_msg="dose, %d slabs" % n_slabs)
+    p = problem()
+    s = ctx.heat_slab(p.thermal, Q, p.traj, 0, 15)
+    buf = torch.empty(s.halo_bytes(), dtype=torch.uint8, device="cuda")
+    with pytest.raises(api.BDError):
+        s.halo_copy(0, 0, buf.data_ptr())     # side 0 of the first slab is the grid's face
+    with pytest.raises(api.BDError):
+        s.advance(101)                        # past the end of the run
+    s.close()
+    with pytest.raises(api.BDError):
+        ctx.heat_slab(p.thermal, Q, p.traj, 10, 11)   # fewer than 2 planes
