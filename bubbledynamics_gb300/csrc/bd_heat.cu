@@ -1,5 +1,7 @@
-// Bioheat + CEM43 dose along a scan trajectory: bd_spiral_heat_run and
-// bd_trajectory_shifts.  Replaces T:52-105 (kernel) and T:323-573 (host loop).
+// Bioheat + CEM43 dose along a scan trajectory: bd_spiral_heat_run (one
+// domain, or z slabs of one device: bd_spiral_heat_run_slabs), one rank's z
+// slab (bd_heat_slab_*) and bd_trajectory_shifts.  Replaces T:52-105 (kernel)
+// and T:323-573 (host loop).
 //
 // BD_F64: temperature in double, dose increment pow(4|2, T-43) dt exactly as
 //         T:99-102 (reference-faithful mode).
