@@ -1,5 +1,7 @@
 // Westervelt solver: host driver behind bd_westervelt_run / _begin / _advance /
-// _finish / checkpoints.  Replaces the host program W:350-790.
+// _finish / checkpoints, the z-slab sessions and runs (bd_westervelt_slab_begin,
+// bd_westervelt_run_slabs) and the adjoint (bd_westervelt_adjoint, _slabs).
+// Replaces the host program W:350-790.
 //
 // Device layout (cells x-fastest, W:155):
 //   P[5]          pressure ring; at step s the buffer (4s + k) mod 5 holds p^{s-k}
